@@ -1,0 +1,366 @@
+"""Benchmark: accepted bubble-steps per second of the Durian foam step.
+
+Default workload: 3D periodic foam, N = 1,000,000, FP64, phi = 0.80,
+r ~ Normal(1, 0.15) clipped to [0.3, 2.5], kappa = 0.01, K = 0.1,
+tolerance 1e-5 (seeded synthetic input, uniform positions). One "step" is
+one accepted integrate() step (rejected attempts, neighbour searches and
+deletions inside it are part of its cost).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference's path on the host cores: the
+reference has no CPU implementation, so this is the FP64 OpenMP restatement
+(oracle/) with all host threads, on the same workload.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+METRIC = "bubble-steps/s at 1 GB300, 3D N=1e6: FP64 vs mixed/batched at stated error; HBM %"
+
+
+def workload(name, seed, precision=0, use_graph=1):
+    from cubble_gb300 import workloads
+    if name == "c2":
+        cfg, st = workloads.config_c2(seed=seed, precision=precision, use_graph=use_graph)
+        desc = ("3D periodic foam N=1e6, phi=0.80, r~N(1,0.15) in [0.3,2.5], kappa=0.01, "
+                "K=0.1, tol 1e-5")
+    elif name == "c1":
+        cfg, st = workloads.config_c1(seed=seed, precision=precision, use_graph=use_graph)
+        desc = "2D periodic foam N=1e4, phi=0.90, r~N(1,0.1) in [0.3,2.0], kappa=0.01, K=0.1, tol 1e-5"
+    else:
+        raise SystemExit("unknown workload " + name)
+    return cfg, st, desc
+
+
+def peaks():
+    try:
+        with open(PEAKS_FILE) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for ln in f:
+                parts = [p.strip() for p in ln.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce(x, op, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=op)
+    return float(t.item())
+
+
+def algorithmic_bytes(dim, np_per_n):
+    """Algorithmic HBM bytes per bubble of each attempt kernel (FP64 form)."""
+    if dim == 3:
+        return {"predict": 136.0, "pairs": 80.0 + 8.0 * np_per_n, "correct": 304.0,
+                "step": 224.0 + 8.0 * np_per_n}
+    return {"predict": 104.0, "pairs": 64.0 + 8.0 * np_per_n, "correct": 272.0,
+            "step": 176.0 + 8.0 * np_per_n}
+
+
+def state_bytes(st):
+    return int(sum(np.asarray(v).nbytes for v in st.values()))
+
+
+def pinned_copy(st):
+    """Host copy of the state in pinned (page-locked) memory."""
+    import torch
+    out = {}
+    for k, v in st.items():
+        v = np.ascontiguousarray(v)
+        t = torch.empty(v.shape, dtype=torch.from_numpy(v[:1]).dtype, pin_memory=True)
+        a = t.numpy()
+        a[...] = v
+        out[k] = (a, t)
+    return {k: a for k, (a, _) in out.items()}, [t for _, t in out.values()]
+
+
+def cpu_baseline(cfg, st, steps):
+    from oracle.oracle import OracleFoam
+    from cubble_gb300 import workloads
+    threads = os.cpu_count() or 1
+    f = OracleFoam(cfg, threads=threads)
+    f.load_state(st)
+    workloads.prepare(f)
+    f.integrate(1)
+    r0 = f.report()
+    t0 = time.perf_counter()
+    f.integrate(steps)
+    dt = time.perf_counter() - t0
+    r1 = f.report()
+    bs = r1["bubble_steps"] - r0["bubble_steps"]
+    return bs / dt, threads, steps, dt
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    cfg, st, desc = workload(args.workload, args.seed)
+    from oracle.oracle import OracleFoam
+    from cubble_gb300 import workloads
+    threads = os.cpu_count() or 1
+    f = OracleFoam(cfg, threads=threads)
+    f.load_state(st)
+    workloads.prepare(f)
+    f.integrate(args.warmup)
+    r0 = f.report()
+    steps = args.steps if args.ref_steps is None else min(args.steps, args.ref_steps)
+    t0 = time.perf_counter()
+    f.integrate(steps)
+    el = time.perf_counter() - t0
+    r1 = f.report()
+    bs = r1["bubble_steps"] - r0["bubble_steps"]
+    value = bs / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "bubble-steps/s",
+        "n_gpus": world, "steps": steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * el / max(steps, 1), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, uniform positions)",
+        "config": {"workload": desc, "parallelism": "host threads"},
+        "cpu_baseline": {"value": value, "unit": "bubble-steps/s", "cores": threads,
+                         "kind": "port",
+                         "sample": "%d accepted steps of the full workload after %d warm-up "
+                                   "steps (the reference has no CPU path; FP64 OpenMP "
+                                   "restatement)" % (steps, args.warmup)},
+        "e2e": {"value": value, "unit": "bubble-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "attempts": r1["attempts"] - r0["attempts"],
+        "searches": r1["searches"] - r0["searches"],
+    }
+    print(json.dumps(line))
+
+
+def run_gb300(args, world, rank, local):
+    import torch
+    import cubble_gb300 as cb
+    from cubble_gb300 import workloads
+    torch.cuda.set_device(local)
+    cb.build()
+    cfg, st, desc = workload(args.workload, args.seed + rank, precision=args.precision,
+                             use_graph=args.graph)
+    dim = cfg.dimensionality
+    sim = cb.GpuFoam(cfg)
+    sim.load_state(st)
+    workloads.prepare(sim)
+    sim.integrate(args.warmup)
+    r0 = sim.report()
+    l0 = sim.launch_count()
+    clocks = Clocks(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    r1, dev_ms = sim.integrate_timed(args.steps)
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    launches = sim.launch_count() - l0
+    bs = r1["bubble_steps"] - r0["bubble_steps"]
+    el = allreduce(dev_ms / 1e3, _op("max"), world)
+    bs_all = allreduce(bs, _op("sum"), world)
+    value = bs_all / el
+    attempts = r1["attempts"] - r0["attempts"]
+    searches = r1["searches"] - r0["searches"]
+    np_per_n = r1["num_pairs"] / max(r1["count"], 1)
+    # per-kernel device times (CUDA events on the library's stream)
+    kms = sim.profile_kernels(reps=5)
+    names = ["predict", "pairs", "correct"]
+    top = int(np.argmax(kms))
+    ab = algorithmic_bytes(dim, np_per_n)
+    n_now = r1["count"]
+    hbm, src = peaks()
+    achieved = ab[names[top]] * n_now / (kms[top] * 1e-3) / 1e9
+    step_gbs = ab["step"] * n_now / (sum(kms) * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": names[top], "achieved": achieved, "peak": hbm,
+            "unit": "GB/s", "frac": achieved / hbm, "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs)",
+            "traffic": None,
+            "kernel_ms": dict(zip(names, kms)),
+            "algorithmic_bytes_per_bubble": ab,
+            "step_achieved_gbs": step_gbs, "step_frac": step_gbs / hbm}
+    sim.close()
+
+    # end to end through the C ABI with pinned host buffers: upload, search +
+    # bootstrap, K steps each returning its report to the host, download.
+    e2e = None
+    if not args.no_e2e:
+        host, keep = pinned_copy(st)
+        g2 = cb.GpuFoam(cfg)
+        out = {k: np.empty_like(v) for k, v in host.items()}
+        barrier(world)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g2.load_state(host)
+        workloads.prepare(g2)
+        q0 = g2.report()
+        for _ in range(args.warmup + args.steps):
+            g2.integrate(1)
+        q1 = g2.report()
+        fin = g2.get_state(rows=list(host.keys()))
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        barrier(world)
+        e2e_s = allreduce(e2e_s, _op("max"), world)
+        e2e_bs = allreduce(q1["bubble_steps"] - q0["bubble_steps"], _op("sum"), world)
+        nsteps = args.warmup + args.steps
+        import ctypes
+        rep = ctypes.sizeof(cb._abi.Report)
+        e2e = {"value": e2e_bs / e2e_s, "unit": "bubble-steps/s",
+               "h2d_bytes_per_step": state_bytes(host) // nsteps,
+               "d2h_bytes_per_step": rep + state_bytes(fin) // nsteps,
+               "steps": nsteps, "note": "state upload, search, bootstrap, %d steps each reading "
+                                         "its report back, state download" % nsteps}
+        g2.close()
+        del keep, out
+
+    base = None
+    if rank == 0 and not args.no_cpu:
+        v, cores, n_steps, secs = cpu_baseline(cfg, st, args.cpu_steps)
+        base = {"value": v, "unit": "bubble-steps/s", "cores": cores, "kind": "port",
+                "sample": "%d accepted steps of the same workload after its first step "
+                          "(%.1f s, FP64 OpenMP restatement of the reference step)" % (n_steps, secs)}
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "bubble-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == 0 else "f64/f32 mixed",
+        "data": "synthetic (seeded, uniform positions)",
+        "config": {"workload": desc, "precision": "fp64" if args.precision == 0 else "mixed",
+                   "graph": bool(args.graph), "parallelism": "replicas" if world > 1 else "single foam",
+                   "l2": "working set larger than L2 (state + pairs > 129 MB)",
+                   "attempts": attempts, "searches": searches,
+                   "pairs_per_bubble": np_per_n, "bubbles_end": r1["count"],
+                   "deleted": r1["deleted"] - r0["deleted"], "dt_end": r1["time_step"]},
+        "roofline": roof, "cpu_baseline": base, "e2e": e2e, "gpu_launches": launches,
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+
+
+def _op(name):
+    try:
+        import torch.distributed as dist
+        return {"max": dist.ReduceOp.MAX, "sum": dist.ReduceOp.SUM}[name]
+    except Exception:
+        return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="c2")
+    ap.add_argument("--precision", type=int, default=0)
+    ap.add_argument("--graph", type=int, default=1)
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--cpu-steps", type=int, default=30)
+    ap.add_argument("--ref-steps", type=int, default=200)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        # the CPU arm needs no process group: rank 0 works, the others exit
+        world = int(os.environ.get("WORLD_SIZE", "1"))
+        run_reference(args, world, int(os.environ.get("RANK", "0")))
+        return
+    world, rank, local = dist_setup()
+    if False:
+        pass
+    else:
+        run_gb300(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,276 @@
+// Shared device-side definitions of the GB300 Durian foam step.
+//
+// Memory layout in HBM (one context):
+//   * persistent per-bubble rows are FP64 / int32 SoA "slots" of `capacity`
+//     elements; which slot plays which role (current x, corrected x, the
+//     three velocity generations, ...) lives in the device control block, so
+//     buffer rotation after an accepted step (src/simulator.cu:258-301) and
+//     the cell-order permutation of a search (src/simulator.cu:96-147) are
+//     role swaps done on the device; no host round trip is needed;
+//   * `pred` packs the predicted state of a bubble into one 32-byte sector
+//     (3D: xp,yp,zp,rp; 2D: xp,yp,rp,1/rp) because the pair kernel gathers
+//     it for both members of every pair;
+//   * `acc` holds 8 FP64 accumulators per bubble (64 bytes: vx,vy,vz,vr,
+//     overlap, flow vx,vy,vz) that the pair kernel adds into with FP64
+//     atomics; it is all zero between attempts (the correct kernel reads
+//     and clears it);
+//   * pairs are two int32 rows (i, j), double-buffered for compaction.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/cubble_gb300.h"
+
+namespace cbg {
+
+constexpr double kPi = 3.1415926535897932384626433832795028841971693993;
+constexpr int kBlock = 256;  // threads per block of every grid-stride kernel
+constexpr int kAcc = 8;      // FP64 accumulators per bubble
+constexpr int kPartSlots = 8;
+
+// Double-row roles (slot table indices are in Ctrl::drole).
+enum DRole : int {
+    RX = 0, RY, RZ, RR,          // current position and radius
+    RXN, RYN, RZN, RRN,          // corrected (next) position and radius
+    RV0, RV1, RV2, RV3,          // dxdt, dydt, dzdt, drdt
+    RVO0, RVO1, RVO2, RVO3,      // dxdto ... (previous step)
+    RVP0, RVP1, RVP2, RVP3,      // dxdtp ... (this attempt)
+    RPATH, RPATHN, RERR, RERR2,  // path, pathNew, error, spare
+    RS0, RS1, RS2, RS3,          // saved position / radius of the last search
+    ND_ROLES
+};
+enum IRole : int {
+    IWX = 0, IWY, IWZ, IIDX, INN,  // wrap counts, index, numNeighbors
+    IWX2, IWY2, IWZ2, IIDX2,       // spares for the permutation
+    NI_ROLES
+};
+enum PRole : int { PI0 = 0, PJ0, PI1, PJ1, NP_ROLES };
+
+// Counters of the "last block finishes the reduction" pattern.
+enum DoneCounter : int {
+    DC_PREDICT = 0, DC_PAIRS, DC_CORRECT, DC_WRAP, DC_PERMUTE, DC_REMOVE,
+    DC_SCAN, DC_MISC, DC_COUNT
+};
+
+// Values that change only through cb_set_box / cb_create.
+struct DevConst {
+    int dim;
+    int wall[3];
+    int any_wall;
+    int max_attempts;
+    int cap, pcap, ccap;
+    int pad_;
+    double lbb[3], tfr[3], iv[3];
+    double flow_lbb[3], flow_tfr[3], flow_vel[3];
+    double wall_drag, min_rad, f0, K, kappa, skin, vol_mul_const, ain, tol;
+    float pre_margin;  // FP32 pair-search prefilter margin (length units)
+    float half_iv32[3];
+    float iv32[3];
+};
+
+// Device control block. The host reads it after each eager phase or at the
+// end of a graph launch (one small copy).
+struct Ctrl {
+    int n, np, ndel, status;
+    int use_gas, use_flow, inc_path, graph_mode;
+    double dt;
+    double sumA, sumAr, sumAo, sumAor;
+    double max_err, max_rad, max_exp, vol_new;
+    double max_bubble_radius;
+    int too_large, need_search, need_delete, attempts_this_step;
+    unsigned long long tint;
+    double tfrac;
+    long long steps, attempts, searches, deleted, bubble_steps;
+    long long steps_target;
+    long long delete_events;  // removeBubbles() calls
+    unsigned long long h_loop, h_delete, h_search;  // conditional handles
+    int drole[ND_ROLES];
+    int irole[NI_ROLES];
+    int prole[NP_ROLES];
+    int cell_dims[3];
+    int ncell;
+    int nnew;
+    int np_found;        // pairs found by the last search (may exceed capacity)
+    int no_accept;       // cb_attempt: decide dt but do not accept
+    double misc_result;  // energy / volume results
+    unsigned int done[DC_COUNT];
+};
+
+// Every device buffer of a context; kernels take it by value.
+struct Bufs {
+    Ctrl *ctrl;
+    const DevConst *k;
+    double *const *ds;  // double slots
+    int *const *is;     // int slots
+    int *const *ps;     // pair slots
+    double *pred;       // 4 doubles per bubble
+    double *invr;       // 1 / rp (3D)
+    double *acc;        // kAcc doubles per bubble
+    double *part;       // kPartSlots x grid partials
+    int *delflag;       // deletion marks of the last attempt
+    int *iscan;         // cap + 1 scan output
+    int *blocksums;     // grid + 1
+    int *cellOf;        // cell of each bubble (old order)
+    int *cellSorted;    // cell of each bubble (cell order)
+    int *perm;          // new position -> old position (atomic order)
+    int *permSorted;    // new position -> old position (sorted in cell)
+    int *cellCount;     // ccap + 1
+    int *cellStart;     // ccap + 1
+    int *cellFill;      // ccap + 1
+    int *rowCount;      // cap + 1
+    int *rowStart;      // cap + 1
+    float4 *pos32;      // FP32 copy of x, y, z, r for the search prefilter
+    int *holes;         // cap
+    int *moveDst;       // cap
+    int *keep;          // pcap + 1
+    int *keepScan;      // pcap + 1
+    double *dbg_ov;     // optional copy of the overlap row (cb_attempt)
+    double *energy;     // per-bubble energies
+};
+
+// ------------------------------------------------------------- helpers
+__device__ __forceinline__ double *drow(const Bufs &b, const Ctrl *c, int role) {
+    return b.ds[c->drole[role]];
+}
+__device__ __forceinline__ int *irow(const Bufs &b, const Ctrl *c, int role) {
+    return b.is[c->irole[role]];
+}
+
+// Deterministic block reduction (fixed tree for a fixed blockDim).
+template <typename Op>
+__device__ __forceinline__ double block_reduce(double v, Op op, double *smem,
+                                               double identity = 0.0) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_down_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if (lane == 0) smem[warp] = v;
+    __syncthreads();
+    const int nw = blockDim.x >> 5;
+    double r = 0.0;
+    if (warp == 0) {
+        r = lane < nw ? smem[lane] : identity;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r = op(r, __shfl_down_sync(0xffffffffu, r, o));
+    }
+    return r;  // valid in thread 0
+}
+
+struct OpSum {
+    __device__ __forceinline__ double operator()(double a, double b) const { return a + b; }
+};
+struct OpMax {
+    __device__ __forceinline__ double operator()(double a, double b) const { return fmax(a, b); }
+};
+
+__device__ __forceinline__ int block_reduce_int(int v, int *smem) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if (lane == 0) smem[warp] = v;
+    __syncthreads();
+    const int nw = blockDim.x >> 5;
+    int r = 0;
+    if (warp == 0) {
+        r = lane < nw ? smem[lane] : 0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+    }
+    return r;
+}
+
+// "Last block" pattern: every block publishes its partials, fences, and the
+// block that finishes last does the final (deterministic, in-order)
+// reduction. No block ever waits on another, so nothing can hang.
+__device__ __forceinline__ bool last_block(unsigned int *counter) {
+    __shared__ bool am_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned int prev = atomicAdd(counter, 1u);
+        am_last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (am_last) __threadfence();
+    return am_last;
+}
+
+// Sum / max of this kernel's partials in block order (last block only).
+__device__ __forceinline__ double fold_partials(const double *p, int nblocks, bool is_max,
+                                                double *smem) {
+    double v = 0.0;  // identity of both (all maxima here are of values >= 0)
+    // each thread folds a strided subset in order, then a fixed tree
+    for (int k = threadIdx.x; k < nblocks; k += blockDim.x) {
+        const double t = __ldcg(p + k);
+        v = is_max ? fmax(v, t) : v + t;
+    }
+    return is_max ? block_reduce(v, OpMax(), smem) : block_reduce(v, OpSum(), smem);
+}
+
+// wrappedDifference, src/kernels.cu:1094-1114 (minimum image on periodic axes)
+template <int DIM>
+__device__ __forceinline__ void wrapped_diff(const DevConst &k, double x1, double y1, double z1,
+                                             double x2, double y2, double z2, double &dx,
+                                             double &dy, double &dz) {
+    const double d1x = x1 - x2, d1y = y1 - y2, d1z = DIM == 3 ? z1 - z2 : 0.0;
+    dx = d1x;
+    dy = d1y;
+    dz = d1z;
+    const double tx = k.iv[0] - fabs(d1x);
+    const double ty = k.iv[1] - fabs(d1y);
+    if (!k.wall[0] && tx * tx < d1x * d1x) dx = d1x < 0 ? tx : -tx;
+    if (!k.wall[1] && ty * ty < d1y * d1y) dy = d1y < 0 ? ty : -ty;
+    if (DIM == 3) {
+        const double tz = k.iv[2] - fabs(d1z);
+        if (!k.wall[2] && tz * tz < d1z * d1z) dz = d1z < 0 ? tz : -tz;
+    }
+}
+
+// Same, with every operation rounded separately (no contraction), so the
+// pair acceptance test is bit-identical to the oracle's.
+template <int DIM>
+__device__ __forceinline__ double exact_sqdist(const DevConst &k, double x1, double y1, double z1,
+                                               double x2, double y2, double z2) {
+    const double d1x = __dsub_rn(x1, x2), d1y = __dsub_rn(y1, y2);
+    const double d1z = DIM == 3 ? __dsub_rn(z1, z2) : 0.0;
+    double dx = d1x, dy = d1y, dz = d1z;
+    const double tx = __dsub_rn(k.iv[0], fabs(d1x));
+    const double ty = __dsub_rn(k.iv[1], fabs(d1y));
+    if (!k.wall[0] && __dmul_rn(tx, tx) < __dmul_rn(d1x, d1x)) dx = d1x < 0 ? tx : -tx;
+    if (!k.wall[1] && __dmul_rn(ty, ty) < __dmul_rn(d1y, d1y)) dy = d1y < 0 ? ty : -ty;
+    if (DIM == 3) {
+        const double tz = __dsub_rn(k.iv[2], fabs(d1z));
+        if (!k.wall[2] && __dmul_rn(tz, tz) < __dmul_rn(d1z, d1z)) dz = d1z < 0 ? tz : -tz;
+    }
+    double t = __dmul_rn(dx, dx);
+    t = __dadd_rn(t, __dmul_rn(dy, dy));
+    t = __dadd_rn(t, __dmul_rn(dz, dz));
+    return t;
+}
+
+// ------------------------------------------------------ kernel launchers
+struct Launch {
+    int grid;         // blocks of every grid-stride kernel (multiple of #SMs)
+    int scan_grid;    // blocks of the scan kernels
+    cudaStream_t stream;
+    long long *launches;  // host-side launch counter
+};
+
+// step.cu
+void launch_predict(const Launch &l, const Bufs &b, int dim);
+void launch_pairs(const Launch &l, const Bufs &b, int dim, int mode);  // mode: 0 step, 1 bootstrap
+void launch_correct(const Launch &l, const Bufs &b, int dim);
+void launch_boot(const Launch &l, const Bufs &b, int dim, int phase);
+void launch_energy(const Launch &l, const Bufs &b, int dim, int per_bubble);
+void launch_volume(const Launch &l, const Bufs &b, int dim);
+// search.cu
+void launch_search(const Launch &l, const Bufs &b, int dim);
+// remove.cu
+void launch_remove(const Launch &l, const Bufs &b, int dim);
+// scan.cu
+void launch_scan(const Launch &l, const Bufs &b, const int *in, int *out, const int *count_ptr,
+                 int count_add, int *total_out);
+
+}  // namespace cbg

@@ -1,0 +1,639 @@
+// One attempt of the Adams-Bashforth-Moulton step, FP64 form:
+//   k_predict  : AB2 predict of x, y, (z), r into the packed `pred` rows and
+//                the area sums (preIntegrate, src/kernels.cu:40-170)
+//   k_pairs    : overlap velocities, pairwise gas flux, overlap areas and
+//                flow neighbour sums per pair (pairwiseInteraction,
+//                src/kernels.cu:172-337)
+//   k_correct  : flow and wall velocities, the mean-field gas exchange, AM2
+//                correct, error / expansion / radius maxima, deletion marks,
+//                path; its last block takes the accept/reject decision and
+//                the dt update of step() (src/simulator.cu:219-246) and, on
+//                accept, rotates the buffers and advances the clock as
+//                integrate() does (src/simulator.cu:258-334) — on the device
+//                (postIntegrate, correct, addFlowVelocity, addWallVelocity,
+//                src/kernels.cu:339-593)
+// plus the Euler bootstrap of init() (src/simulator.cu:727-787) and the
+// energy / volume reductions (src/kernels.cu:941-957, :1013-1024).
+#include "common.cuh"
+
+namespace cbg {
+namespace {
+
+__device__ __forceinline__ void swap_role(int *r, int a, int b) {
+    const int t = r[a];
+    r[a] = r[b];
+    r[b] = t;
+}
+
+__device__ __forceinline__ void set_cond(unsigned long long h, unsigned int v) {
+    cudaGraphSetConditional((cudaGraphConditionalHandle)h, v);
+}
+
+__device__ __forceinline__ double4_32a ld4(const double *p, int i) {
+    return reinterpret_cast<const double4_32a *>(p)[i];
+}
+
+// ---------------------------------------------------------------- predict
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_predict(Bufs b) {
+    __shared__ double smem[32];
+    const Ctrl *c = b.ctrl;
+    const int n = c->n;
+    const double ts = c->dt;
+    const int gas = c->use_gas;
+    const double *X = drow(b, c, RX), *Y = drow(b, c, RY), *Z = drow(b, c, RZ),
+                 *R = drow(b, c, RR);
+    const double *V0 = drow(b, c, RV0), *V1 = drow(b, c, RV1), *V2 = drow(b, c, RV2),
+                 *V3 = drow(b, c, RV3);
+    const double *O0 = drow(b, c, RVO0), *O1 = drow(b, c, RVO1), *O2 = drow(b, c, RVO2),
+                 *O3 = drow(b, c, RVO3);
+    double sA = 0.0, sAr = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        // p + 0.5 ts (3 v - vo), src/kernels.cu:48-50
+        const double xp = X[i] + 0.5 * ts * (3.0 * V0[i] - O0[i]);
+        const double yp = Y[i] + 0.5 * ts * (3.0 * V1[i] - O1[i]);
+        double rp = R[i];
+        if (gas) rp = R[i] + 0.5 * ts * (3.0 * V3[i] - O3[i]);
+        const double inv = 1.0 / rp;
+        double4_32a p;
+        if (DIM == 3) {
+            p.x = xp;
+            p.y = yp;
+            p.z = Z[i] + 0.5 * ts * (3.0 * V2[i] - O2[i]);
+            p.w = rp;
+            b.invr[i] = inv;
+        } else {
+            p.x = xp;
+            p.y = yp;
+            p.z = rp;
+            p.w = inv;
+        }
+        reinterpret_cast<double4_32a *>(b.pred)[i] = p;
+        if (gas) {  // area and area per radius, src/kernels.cu:103-112
+            double apr = 2.0 * kPi;
+            if (DIM == 3) apr *= 2.0 * rp;
+            sA += apr * rp;
+            sAr += apr;
+        }
+    }
+    const double tA = block_reduce(sA, OpSum(), smem);
+    const double tAr = block_reduce(sAr, OpSum(), smem);
+    if (threadIdx.x == 0) {
+        b.part[0 * gridDim.x + blockIdx.x] = tA;
+        b.part[1 * gridDim.x + blockIdx.x] = tAr;
+    }
+    if (last_block(&b.ctrl->done[DC_PREDICT])) {
+        const double fA = fold_partials(b.part + 0 * gridDim.x, gridDim.x, false, smem);
+        const double fAr = fold_partials(b.part + 1 * gridDim.x, gridDim.x, false, smem);
+        if (threadIdx.x == 0) {
+            b.ctrl->sumA = fA;
+            b.ctrl->sumAr = fAr;
+            b.ctrl->done[DC_PREDICT] = 0;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ pairs
+// One lane per pair; contributions to both members go through FP64 atomics
+// into the per-bubble accumulator rows.
+template <int DIM, bool GAS, bool FLOW>
+__global__ void __launch_bounds__(kBlock) k_pairs(Bufs b) {
+    __shared__ double smem[32];
+    const Ctrl *c = b.ctrl;
+    const DevConst &k = *b.k;
+    const int np = c->np;
+    const int *PI = b.ps[c->prole[PI0]];
+    const int *PJ = b.ps[c->prole[PJ0]];
+    const double *V0 = drow(b, c, RV0), *V1 = drow(b, c, RV1), *V2 = drow(b, c, RV2);
+    const double f0 = k.f0;
+    double sAo = 0.0, sAor = 0.0;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+        const int i = PI[p], j = PJ[p];
+        double *ai = b.acc + (size_t)i * kAcc;
+        double *aj = b.acc + (size_t)j * kAcc;
+        if (FLOW) {  // src/kernels.cu:191-207 (added for every pair)
+            atomicAdd(aj + 5, V0[i]);
+            atomicAdd(aj + 6, V1[i]);
+            if (DIM == 3) atomicAdd(aj + 7, V2[i]);
+        }
+        const double4_32a a = ld4(b.pred, i), q = ld4(b.pred, j);
+        double r1, r2, zi = 0.0, zj = 0.0, inv1, inv2;
+        if (DIM == 3) {
+            zi = a.z;
+            zj = q.z;
+            r1 = a.w;
+            r2 = q.w;
+            inv1 = inv2 = 0.0;
+        } else {
+            r1 = a.z;
+            r2 = q.z;
+            inv1 = a.w;
+            inv2 = q.w;
+        }
+        const double radii = r1 + r2;
+        double dx, dy, dz;
+        wrapped_diff<DIM>(k, a.x, a.y, zi, q.x, q.y, zj, dx, dy, dz);
+        double m = dx * dx + dy * dy;
+        if (DIM == 3) m += dz * dz;
+        if (radii * radii >= m) {
+            // velocity, src/kernels.cu:218-233
+            const double s = f0 * (rsqrt(m) - 1.0 / radii);
+            const double fx = dx * s, fy = dy * s;
+            atomicAdd(ai + 0, fx);
+            atomicAdd(aj + 0, -fx);
+            atomicAdd(ai + 1, fy);
+            atomicAdd(aj + 1, -fy);
+            if (DIM == 3) {
+                const double fz = dz * s;
+                atomicAdd(ai + 2, fz);
+                atomicAdd(aj + 2, -fz);
+            }
+            if (GAS) {  // pairwise gas exchange, src/kernels.cu:236-280
+                const double r1sq = r1 * r1, r2sq = r2 * r2;
+                double oa;
+                if (m < r1sq || m < r2sq) {
+                    oa = r1sq < r2sq ? r1sq : r2sq;
+                } else {
+                    oa = 0.5 * (r2sq - r1sq + m);
+                    oa *= oa;
+                    oa /= m;
+                    oa = r2sq - oa;
+                    oa = oa < 0 ? -oa : oa;
+                }
+                if (DIM == 3) {
+                    oa *= kPi;
+                    inv1 = b.invr[i];
+                    inv2 = b.invr[j];
+                } else {
+                    oa = 2.0 * sqrt(oa);
+                }
+                const double g = oa * (inv2 - inv1);
+                atomicAdd(ai + 3, g);
+                atomicAdd(aj + 3, -g);
+                atomicAdd(ai + 4, oa);
+                atomicAdd(aj + 4, oa);
+                sAo += 2.0 * oa;
+                sAor += oa * (inv1 + inv2);
+            }
+            if (FLOW) {  // src/kernels.cu:298-307 (overlapping pairs only)
+                atomicAdd(ai + 5, V0[j]);
+                atomicAdd(ai + 6, V1[j]);
+                if (DIM == 3) atomicAdd(ai + 7, V2[j]);
+            }
+        }
+    }
+    const double tAo = block_reduce(sAo, OpSum(), smem);
+    const double tAor = block_reduce(sAor, OpSum(), smem);
+    if (threadIdx.x == 0) {
+        b.part[2 * gridDim.x + blockIdx.x] = tAo;
+        b.part[3 * gridDim.x + blockIdx.x] = tAor;
+    }
+    if (last_block(&b.ctrl->done[DC_PAIRS])) {
+        const double fAo = fold_partials(b.part + 2 * gridDim.x, gridDim.x, false, smem);
+        const double fAor = fold_partials(b.part + 3 * gridDim.x, gridDim.x, false, smem);
+        if (threadIdx.x == 0) {
+            b.ctrl->sumAo = fAo;
+            b.ctrl->sumAor = fAor;
+            b.ctrl->done[DC_PAIRS] = 0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- correct
+// touchesWall, src/kernels.cu:553-566
+__device__ __forceinline__ bool touches_wall(double f0, double rad, double x, double low,
+                                             double high, double &velocity) {
+    double d1 = x - low;
+    double d2 = x - high;
+    d1 = d1 * d1 < d2 * d2 ? d1 : d2;
+    if (rad * rad >= d1 * d1) {
+        d2 = d1 < 0.0 ? -1.0 : 1.0;
+        d1 *= d2;
+        velocity = d2 * f0 * (1.0 - d1 / rad);
+        return true;
+    }
+    return false;
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_correct(Bufs b) {
+    __shared__ double smem[32];
+    __shared__ int ismem[32];
+    Ctrl *c = b.ctrl;
+    const DevConst &k = *b.k;
+    const int n = c->n;
+    const double ts = c->dt;
+    const int gas = c->use_gas, flow = c->use_flow, path = c->inc_path;
+    const double *X = drow(b, c, RX), *Y = drow(b, c, RY), *Z = drow(b, c, RZ),
+                 *R = drow(b, c, RR);
+    double *XN = drow(b, c, RXN), *YN = drow(b, c, RYN), *ZN = drow(b, c, RZN),
+           *RN = drow(b, c, RRN);
+    const double *V0 = drow(b, c, RV0), *V1 = drow(b, c, RV1), *V2 = drow(b, c, RV2),
+                 *V3 = drow(b, c, RV3);
+    double *P0 = drow(b, c, RVP0), *P1 = drow(b, c, RVP1), *P2 = drow(b, c, RVP2),
+           *P3 = drow(b, c, RVP3);
+    const double *S0 = drow(b, c, RS0), *S1 = drow(b, c, RS1), *S2 = drow(b, c, RS2),
+                 *S3 = drow(b, c, RS3);
+    const double *PATH = drow(b, c, RPATH);
+    double *PATHN = drow(b, c, RPATHN), *ERR = drow(b, c, RERR);
+    const int *NN = irow(b, c, INN);
+    // mean-field factors, src/kernels.cu:399-404 (uniform over bubbles)
+    const double sA = c->sumA, sAr = c->sumAr, sAo = c->sumAo, sAor = c->sumAor;
+    const double mfa = (sAr - sAor) / (sA - sAo);
+    const double mfb = k.kappa * k.ain * (double)n / sA;
+    const double drag = 1.0 - k.wall_drag;
+    double merr = 0.0, mrad = 0.0, mexp = 0.0, vol = 0.0;
+    int ndel = 0, bad = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double *acc = b.acc + (size_t)i * kAcc;
+        const double4_32a a0 = reinterpret_cast<const double4_32a *>(acc)[0];
+        double4_32a a1;
+        a1.x = a1.y = a1.z = a1.w = 0.0;
+        if (gas || flow) a1 = reinterpret_cast<const double4_32a *>(acc)[1];
+        double vpx = a0.x, vpy = a0.y, vpz = a0.z, vpr = a0.w;
+        const double ov = a1.x;
+        const double4_32a p = ld4(b.pred, i);
+        const double xp = p.x, yp = p.y, zp = DIM == 3 ? p.z : 0.0, rp = DIM == 3 ? p.w : p.z;
+        if (flow) {  // addFlowVelocity, src/kernels.cu:497-544
+            double multiplier = NN[i];
+            multiplier = (multiplier > 0 ? 1.0 / multiplier : 0.0);
+            const double riSq = rp * rp;
+            int inside = (int)((xp < k.flow_tfr[0] && xp > k.flow_lbb[0]) ||
+                               ((k.flow_lbb[0] - xp) * (k.flow_lbb[0] - xp) <= riSq) ||
+                               ((k.flow_tfr[0] - xp) * (k.flow_tfr[0] - xp) <= riSq));
+            inside *= (int)((yp < k.flow_tfr[1] && yp > k.flow_lbb[1]) ||
+                            ((k.flow_lbb[1] - yp) * (k.flow_lbb[1] - yp) <= riSq) ||
+                            ((k.flow_tfr[1] - yp) * (k.flow_tfr[1] - yp) <= riSq));
+            if (DIM == 3) {
+                inside *= (int)((zp < k.flow_tfr[2] && zp > k.flow_lbb[2]) ||
+                                ((k.flow_lbb[2] - zp) * (k.flow_lbb[2] - zp) <= riSq) ||
+                                ((k.flow_tfr[2] - zp) * (k.flow_tfr[2] - zp) <= riSq));
+                vpz += !inside * multiplier * a1.w + k.flow_vel[2] * inside;
+            }
+            vpx += !inside * multiplier * a1.y + k.flow_vel[0] * inside;
+            vpy += !inside * multiplier * a1.z + k.flow_vel[1] * inside;
+        }
+        if (k.any_wall) {  // addWallVelocity, src/kernels.cu:546-593
+            double xDrag = 1.0, yDrag = 1.0, velocity = 0.0;
+            if (k.wall[0] && touches_wall(k.f0, rp, xp, k.lbb[0], k.tfr[0], velocity)) {
+                vpx += velocity;
+                vpy *= drag;
+                vpz *= drag;
+                xDrag = drag;
+            }
+            velocity = 0.0;
+            if (k.wall[1] && touches_wall(k.f0, rp, yp, k.lbb[1], k.tfr[1], velocity)) {
+                vpx *= drag;
+                vpy += velocity * xDrag;
+                vpz *= drag;
+                yDrag = drag;
+            }
+            velocity = 0.0;
+            if (k.wall[2] && touches_wall(k.f0, rp, zp, k.lbb[2], k.tfr[2], velocity)) {
+                vpx *= drag;
+                vpy *= drag;
+                vpz += velocity * xDrag * yDrag;
+            }
+        }
+        // AM2 correct, src/kernels.cu:487-495 and :366-387
+        double e = 0.0, dist = 0.0, t;
+        const double x0 = X[i], y0 = Y[i];
+        const double cx = x0 + 0.5 * ts * (V0[i] + vpx);
+        e = fmax(e, fabs(xp - cx));
+        t = cx - S0[i];
+        dist += t * t;
+        const double cy = y0 + 0.5 * ts * (V1[i] + vpy);
+        e = fmax(e, fabs(yp - cy));
+        t = cy - S1[i];
+        dist += t * t;
+        double cz = 0.0, z0 = 0.0;
+        if (DIM == 3) {
+            z0 = Z[i];
+            cz = z0 + 0.5 * ts * (V2[i] + vpz);
+            e = fmax(e, fabs(zp - cz));
+            t = cz - S2[i];
+            dist += t * t;
+        }
+        dist = sqrt(dist);
+        int del = 0;
+        if (gas) {  // mean-field gas exchange and radius, src/kernels.cu:390-431
+            double area = 2.0 * kPi * rp;
+            if (DIM == 3) area *= 2.0 * rp;
+            double vr = mfa - 1.0 / rp;
+            vr *= mfb * (area - ov);
+            vr += vpr;
+            vr *= k.K / area;
+            vpr = vr;
+            const double cr = R[i] + 0.5 * ts * (V3[i] + vr);
+            e = fmax(e, fabs(rp - cr));
+            dist += cr - S3[i];
+            if (cr > k.min_rad) {
+                double v3 = cr * cr;
+                if (DIM == 3) v3 *= cr;
+                vol += v3;
+            } else {
+                del = 1;
+                ndel++;
+            }
+            mrad = fmax(mrad, cr);
+            RN[i] = cr;
+            P3[i] = vpr;
+            if (!isfinite(cr)) bad = 1;
+        }
+        b.delflag[i] = del;
+        mexp = fmax(mexp, dist);
+        if (path) {  // src/kernels.cu:437-451
+            t = x0 - cx;
+            double d2 = t * t;
+            t = y0 - cy;
+            d2 += t * t;
+            if (DIM == 3) {
+                t = z0 - cz;
+                d2 += t * t;
+            }
+            PATHN[i] = PATH[i] + sqrt(d2);
+        }
+        ERR[i] = fmax(e, ERR[i]);
+        merr = fmax(merr, e);
+        XN[i] = cx;
+        YN[i] = cy;
+        P0[i] = vpx;
+        P1[i] = vpy;
+        if (DIM == 3) {
+            ZN[i] = cz;
+            P2[i] = vpz;
+        }
+        if (!isfinite(cx) || !isfinite(cy) || !isfinite(cz)) bad = 1;
+        if (b.dbg_ov) b.dbg_ov[i] = ov;
+        // leave the accumulators zeroed for the next attempt
+        double4_32a zero;
+        zero.x = zero.y = zero.z = zero.w = 0.0;
+        reinterpret_cast<double4_32a *>(acc)[0] = zero;
+        if (gas || flow) reinterpret_cast<double4_32a *>(acc)[1] = zero;
+    }
+    const double tErr = block_reduce(merr, OpMax(), smem);
+    const double tRad = block_reduce(mrad, OpMax(), smem);
+    const double tExp = block_reduce(mexp, OpMax(), smem);
+    const double tVol = block_reduce(vol, OpSum(), smem);
+    const int tDel = block_reduce_int(ndel, ismem);
+    const int tBad = block_reduce_int(bad, ismem);
+    const int G = gridDim.x;
+    if (threadIdx.x == 0) {
+        b.part[0 * G + blockIdx.x] = tErr;
+        b.part[1 * G + blockIdx.x] = tRad;
+        b.part[2 * G + blockIdx.x] = tExp;
+        b.part[3 * G + blockIdx.x] = tVol;
+        b.part[4 * G + blockIdx.x] = (double)tDel;
+        b.part[5 * G + blockIdx.x] = (double)tBad;
+    }
+    if (!last_block(&c->done[DC_CORRECT])) return;
+    const double fErr = fold_partials(b.part + 0 * G, G, true, smem);
+    const double fRad = fold_partials(b.part + 1 * G, G, true, smem);
+    const double fExp = fold_partials(b.part + 2 * G, G, true, smem);
+    const double fVol = fold_partials(b.part + 3 * G, G, false, smem);
+    const double fDel = fold_partials(b.part + 4 * G, G, false, smem);
+    const double fBad = fold_partials(b.part + 5 * G, G, false, smem);
+    if (threadIdx.x != 0) return;
+    c->done[DC_CORRECT] = 0;
+    c->max_err = fErr;
+    c->max_rad = fRad;
+    c->max_exp = fExp;
+    c->vol_new = fVol;
+    c->ndel = gas ? (int)fDel : 0;
+    c->attempts += 1;
+    c->attempts_this_step += 1;
+    // step(): accept / reject and the new dt, src/simulator.cu:239-246
+    const double tol = k.tol;
+    const int too_large = fErr > tol;
+    const int increase = fErr < 0.45 * tol && c->dt < 10;
+    if (too_large)
+        c->dt *= 0.37;
+    else if (increase)
+        c->dt *= 1.269;
+    c->too_large = too_large;
+    if (fBad > 0.0 || isnan(fErr)) c->status = CB_ERR_NONFINITE;
+    c->need_delete = 0;
+    c->need_search = 0;
+    if (too_large && c->status == CB_OK) {
+        if (c->attempts_this_step >= k.max_attempts) c->status = CB_ERR_MAX_ATTEMPTS;
+        if (c->dt < 1e-300) c->status = CB_ERR_DT_UNDERFLOW;
+    }
+    if (!too_large && !c->no_accept && c->status == CB_OK) {
+        // integrate(): rotation, src/simulator.cu:258-301
+        int *r = c->drole;
+        for (int a = 0; a < DIM; a++) {
+            swap_role(r, RX + a, RXN + a);
+            const int old = r[RVO0 + a];
+            r[RVO0 + a] = r[RV0 + a];
+            r[RV0 + a] = r[RVP0 + a];
+            r[RVP0 + a] = old;
+        }
+        if (gas) {
+            swap_role(r, RR, RRN);
+            const int old = r[RVO3];
+            r[RVO3] = r[RV3];
+            r[RV3] = r[RVP3];
+            r[RVP3] = old;
+        }
+        if (path) swap_role(r, RPATH, RPATHN);
+        c->steps += 1;
+        c->bubble_steps += n;
+        c->attempts_this_step = 0;
+        // time accumulator, src/simulator.cu:311-314
+        c->tfrac += c->dt;
+        c->tint += (unsigned long long)c->tfrac;
+        c->tfrac = c->tfrac - (double)(unsigned long long)c->tfrac;
+        if (gas) {
+            c->max_bubble_radius = fRad;
+            c->need_delete = c->ndel > 0;
+        }
+        c->need_search = fExp >= 0.5 * k.skin;
+    }
+    if (c->graph_mode) {
+        const int ok = c->status == CB_OK;
+        const int accepted = !too_large;
+        set_cond(c->h_delete, ok && accepted && c->need_delete);
+        set_cond(c->h_search, ok && accepted && c->need_search);
+        set_cond(c->h_loop, ok && (too_large || c->steps < c->steps_target));
+    }
+}
+
+// --------------------------------------------------------------- bootstrap
+// phase 0: pred := (x, r), vo := 0, path := 0
+// phase 1: euler pred += acc * dt (src/kernels.cu:959-969), acc := 0
+// phase 2: vo := acc (= F(x + dt F(x))), acc := 0
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_boot(Bufs b, int phase) {
+    const Ctrl *c = b.ctrl;
+    const int n = c->n;
+    const double ts = c->dt;
+    const double *X = drow(b, c, RX), *Y = drow(b, c, RY), *Z = drow(b, c, RZ),
+                 *R = drow(b, c, RR);
+    double *O0 = drow(b, c, RVO0), *O1 = drow(b, c, RVO1), *O2 = drow(b, c, RVO2),
+           *O3 = drow(b, c, RVO3), *PATH = drow(b, c, RPATH);
+    double4_32a *P = reinterpret_cast<double4_32a *>(b.pred);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double *acc = b.acc + (size_t)i * kAcc;
+        if (phase == 0) {
+            double4_32a p;
+            const double r = R[i];
+            p.x = X[i];
+            p.y = Y[i];
+            if (DIM == 3) {
+                p.z = Z[i];
+                p.w = r;
+                b.invr[i] = 1.0 / r;
+            } else {
+                p.z = r;
+                p.w = 1.0 / r;
+            }
+            P[i] = p;
+            O0[i] = O1[i] = O2[i] = O3[i] = 0.0;
+            PATH[i] = 0.0;
+        } else {
+            double4_32a a = reinterpret_cast<double4_32a *>(acc)[0];
+            if (phase == 1) {
+                double4_32a p = P[i];
+                p.x += a.x * ts;
+                p.y += a.y * ts;
+                if (DIM == 3) p.z += a.z * ts;
+                P[i] = p;
+            } else {
+                O0[i] = a.x;
+                O1[i] = a.y;
+                if (DIM == 3) O2[i] = a.z;
+            }
+            a.x = a.y = a.z = a.w = 0.0;
+            reinterpret_cast<double4_32a *>(acc)[0] = a;
+        }
+    }
+}
+
+// ------------------------------------------------------- energy, volume
+// potentialEnergy, src/kernels.cu:941-957, on the current positions.
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_energy(Bufs b, int per_bubble) {
+    __shared__ double smem[32];
+    Ctrl *c = b.ctrl;
+    const DevConst &k = *b.k;
+    const int np = c->np;
+    const int *PI = b.ps[c->prole[PI0]];
+    const int *PJ = b.ps[c->prole[PJ0]];
+    const double *X = drow(b, c, RX), *Y = drow(b, c, RY), *Z = drow(b, c, RZ),
+                 *R = drow(b, c, RR);
+    double tot = 0.0;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+        const int i = PI[p], j = PJ[p];
+        double dx, dy, dz;
+        wrapped_diff<DIM>(k, X[i], Y[i], DIM == 3 ? Z[i] : 0.0, X[j], Y[j], DIM == 3 ? Z[j] : 0.0,
+                          dx, dy, dz);
+        double m = dx * dx + dy * dy;
+        if (DIM == 3) m += dz * dz;
+        double e = R[i] + R[j] - sqrt(m);
+        if (e > 0) {
+            e *= e;
+            tot += 2.0 * e;
+            if (per_bubble) {
+                atomicAdd(b.energy + i, e);
+                atomicAdd(b.energy + j, e);
+            }
+        }
+    }
+    const double t = block_reduce(tot, OpSum(), smem);
+    if (threadIdx.x == 0) b.part[6 * gridDim.x + blockIdx.x] = t;
+    if (last_block(&c->done[DC_MISC])) {
+        const double f = fold_partials(b.part + 6 * gridDim.x, gridDim.x, false, smem);
+        if (threadIdx.x == 0) {
+            c->misc_result = f;
+            c->done[DC_MISC] = 0;
+        }
+    }
+}
+
+// calculateVolumes + sum, src/kernels.cu:1013-1024, src/simulator.cu:362-379
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_volume(Bufs b) {
+    __shared__ double smem[32];
+    Ctrl *c = b.ctrl;
+    const int n = c->n;
+    const double *R = drow(b, c, RR);
+    double tot = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double radius = R[i];
+        double volume = radius * radius * kPi;
+        if (DIM == 3) volume *= radius * 1.33333333333333333333333333;
+        tot += volume;
+    }
+    const double t = block_reduce(tot, OpSum(), smem);
+    if (threadIdx.x == 0) b.part[6 * gridDim.x + blockIdx.x] = t;
+    if (last_block(&c->done[DC_MISC])) {
+        const double f = fold_partials(b.part + 6 * gridDim.x, gridDim.x, false, smem);
+        if (threadIdx.x == 0) {
+            c->misc_result = f;
+            c->done[DC_MISC] = 0;
+        }
+    }
+}
+
+}  // namespace
+
+void launch_predict(const Launch &l, const Bufs &b, int dim) {
+    if (dim == 3)
+        k_predict<3><<<l.grid, kBlock, 0, l.stream>>>(b);
+    else
+        k_predict<2><<<l.grid, kBlock, 0, l.stream>>>(b);
+    *l.launches += 1;
+}
+
+// mode bits: 1 = gas exchange, 2 = flow. mode 0 is the bootstrap form.
+void launch_pairs(const Launch &l, const Bufs &b, int dim, int mode) {
+    const bool gas = mode & 1, flow = mode & 2;
+#define CB_PAIRS(D, G, F) k_pairs<D, G, F><<<l.grid, kBlock, 0, l.stream>>>(b)
+    if (dim == 3) {
+        if (gas && flow) CB_PAIRS(3, true, true);
+        else if (gas) CB_PAIRS(3, true, false);
+        else if (flow) CB_PAIRS(3, false, true);
+        else CB_PAIRS(3, false, false);
+    } else {
+        if (gas && flow) CB_PAIRS(2, true, true);
+        else if (gas) CB_PAIRS(2, true, false);
+        else if (flow) CB_PAIRS(2, false, true);
+        else CB_PAIRS(2, false, false);
+    }
+#undef CB_PAIRS
+    *l.launches += 1;
+}
+
+void launch_correct(const Launch &l, const Bufs &b, int dim) {
+    if (dim == 3)
+        k_correct<3><<<l.grid, kBlock, 0, l.stream>>>(b);
+    else
+        k_correct<2><<<l.grid, kBlock, 0, l.stream>>>(b);
+    *l.launches += 1;
+}
+
+void launch_boot(const Launch &l, const Bufs &b, int dim, int phase) {
+    if (dim == 3)
+        k_boot<3><<<l.grid, kBlock, 0, l.stream>>>(b, phase);
+    else
+        k_boot<2><<<l.grid, kBlock, 0, l.stream>>>(b, phase);
+    *l.launches += 1;
+}
+
+void launch_energy(const Launch &l, const Bufs &b, int dim, int per_bubble) {
+    if (dim == 3)
+        k_energy<3><<<l.grid, kBlock, 0, l.stream>>>(b, per_bubble);
+    else
+        k_energy<2><<<l.grid, kBlock, 0, l.stream>>>(b, per_bubble);
+    *l.launches += 1;
+}
+
+void launch_volume(const Launch &l, const Bufs &b, int dim) {
+    if (dim == 3)
+        k_volume<3><<<l.grid, kBlock, 0, l.stream>>>(b);
+    else
+        k_volume<2><<<l.grid, kBlock, 0, l.stream>>>(b);
+    *l.launches += 1;
+}
+
+}  // namespace cbg

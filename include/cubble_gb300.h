@@ -1,0 +1,219 @@
+/*
+ * cubble_gb300 — C ABI of the GB300 (sm_103a) Durian wet-foam time step.
+ *
+ * The reference (KJLankinen/cubble) exports only `cubble::run(argc, argv)`
+ * (src/simulator.cu:1161-1186); its step boundary is internal:
+ *   step(Params&, IntegrationParams&)        src/simulator.cu:192-249
+ *   integrate(Params&, IntegrationParams&)   src/simulator.cu:251-337
+ *   searchNeighbors(Params&)                 src/simulator.cu:60-178
+ *   removeBubbles(Params&, int)              src/simulator.cu:180-190
+ *   totalEnergy / totalVolume                src/simulator.cu:39-58, 362-379
+ * operating on the device SoA owned by `Params` (src/data_definitions.h:302-343).
+ * This header is that boundary as a plain C ABI: plain pointers and sizes,
+ * `int` status codes (CB_OK == 0) plus cb_last_error(), no exceptions across
+ * the boundary, one host thread per context, context-owned device memory and
+ * caller-owned host buffers.
+ *
+ * Each entry point below names the reference function or data it replaces.
+ */
+#ifndef CUBBLE_GB300_H
+#define CUBBLE_GB300_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define CB_API __attribute__((visibility("default")))
+#else
+#define CB_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define CB_OK 0
+#define CB_ERR_INVALID_ARGUMENT 1 /* bad pointer, size or configuration      */
+#define CB_ERR_CUDA 2             /* a CUDA runtime call failed               */
+#define CB_ERR_CAPACITY 3         /* bubble, pair or cell capacity exceeded   */
+#define CB_ERR_MAX_ATTEMPTS 4     /* reject loop hit cb_config.max_attempts   */
+#define CB_ERR_NONFINITE 5        /* NaN/Inf in the predictor-corrector error */
+#define CB_ERR_DT_UNDERFLOW 6     /* time step fell below 1e-300              */
+#define CB_ERR_NO_DEVICE 7        /* no CUDA device / extension unusable      */
+#define CB_ERR_STATE 8            /* call made in the wrong order             */
+
+#define CB_PRECISION_FP64 0  /* plain FP64 form (reference arithmetic)        */
+#define CB_PRECISION_MIXED 1 /* FP32 pair geometry on exact 32-bit fixed-point
+                                differences, FP64 positions/volume/error     */
+
+/* ------------------------------------------------------------ constants */
+/* Mirrors `Constants` (src/data_definitions.h:183-225) plus the host-side
+ * knobs of `HostData`/`IntegrationParams` that the step reads
+ * (src/data_definitions.h:227-269). All values are the final device values:
+ * flow_vel is already multiplied by f0/mu0 and flow_lbb/flow_tfr are absolute
+ * coordinates, as after src/simulator.cu:569-570 and :806-811. */
+typedef struct cb_config {
+    int32_t dimensionality;  /* 2 or 3                                     */
+    int32_t wall[3];         /* x, y, z: 1 = wall, 0 = periodic            */
+    int32_t use_gas_exchange;/* IntegrationParams.useGasExchange           */
+    int32_t use_flow;        /* IntegrationParams.useFlow                  */
+    int32_t increment_path;  /* IntegrationParams.incrementPath            */
+    int32_t capacity;        /* maximum number of bubbles                  */
+    int32_t pair_capacity;   /* maximum number of pairs; 0 = 16 (3D) / 8 (2D) per bubble */
+    int32_t max_attempts;    /* reject-loop cap per step; 0 = 64           */
+    int32_t precision;       /* CB_PRECISION_*                             */
+    int32_t use_graph;       /* 1 = run cb_integrate as one CUDA graph with
+                                device-side conditional loops              */
+    double lbb[3];           /* lower back bottom corner of the box        */
+    double tfr[3];           /* top front right corner of the box          */
+    double flow_lbb[3];
+    double flow_tfr[3];
+    double flow_vel[3];
+    double wall_drag;        /* wallDragStrength                           */
+    double min_rad;          /* deletion threshold                         */
+    double f0_per_mu0;       /* fZeroPerMuZero                             */
+    double k_parameter;      /* K                                          */
+    double kappa;            /* kappa                                      */
+    double skin_radius;      /* Verlet skin                                */
+    double bubble_volume_multiplier; /* M of the volume fix                */
+    double average_surface_area_in;  /* <A_in>                             */
+    double error_tolerance;  /* HostData.errorTolerance                    */
+    double time_step;        /* initial dt (HostData.timeStep)             */
+} cb_config;
+
+/* Host view of the persistent per-bubble state, keyed by the bubble order of
+ * the context (cell order after a search). Mirrors the persistent rows of
+ * `Bubbles` (src/data_definitions.h:41-153). Any pointer may be NULL: on
+ * load a NULL row is zero-filled (saved_* default to the positions, index to
+ * 0..count-1), on get a NULL row is skipped. */
+typedef struct cb_state_view {
+    int32_t count;
+    int32_t pad_;
+    double *x, *y, *z, *r;
+    double *dxdt, *dydt, *dzdt, *drdt;     /* current velocities   */
+    double *dxdto, *dydto, *dzdto, *drdto; /* previous velocities  */
+    double *path, *error;
+    double *saved_x, *saved_y, *saved_z, *saved_r;
+    int32_t *wrap_count_x, *wrap_count_y, *wrap_count_z;
+    int32_t *index, *num_neighbors;
+} cb_state_view;
+
+/* Host scalars of the step loop (HostData + IntegrationParams results). */
+typedef struct cb_report {
+    int64_t steps;          /* accepted steps (numIntegrationSteps)        */
+    int64_t attempts;       /* step() calls including rejected ones        */
+    int64_t searches;       /* neighbour searches (numNeighborsSearched)   */
+    int64_t deleted;        /* bubbles removed                             */
+    int64_t bubble_steps;   /* sum over accepted steps of the bubble count */
+    uint64_t time_integer;  /* HostData.timeInteger                        */
+    double time_fraction;   /* HostData.timeFraction                       */
+    double time_step;       /* dt of the next attempt                      */
+    double max_error;       /* of the last attempt                         */
+    double max_radius;      /* HostData.maxBubbleRadius                    */
+    double max_expansion;   /* of the last attempt                         */
+    int32_t count;          /* bubbles                                     */
+    int32_t num_pairs;      /* pairs                                       */
+    int32_t status;         /* CB_* status of the device control block     */
+    int32_t pad_;
+} cb_report;
+
+/* Outputs of one step() attempt (src/simulator.cu:192-249), before the
+ * accept/rotate of integrate(). Row pointers may be NULL (skipped). */
+typedef struct cb_attempt_view {
+    double *xp, *yp, *zp, *rp;             /* corrected values            */
+    double *dxdtp, *dydtp, *dzdtp, *drdtp; /* new velocities              */
+    double *error;                         /* error row after the attempt */
+    double *path_new;                      /* pathNew row                 */
+    double *overlap;                       /* per-bubble overlap area     */
+    int32_t *delete_flags;                 /* 1 where r <= min_rad        */
+    double total_area;                     /* dTotalArea                  */
+    double total_area_per_radius;          /* dTotalAreaPerRadius         */
+    double total_overlap_area;             /* dTotalOverlapArea           */
+    double total_overlap_area_per_radius;  /* dTotalOverlapAreaPerRadius  */
+    double total_volume_new;               /* dTotalVolumeNew             */
+    double max_error, max_radius, max_expansion;
+    int32_t num_to_be_deleted;             /* dNumToBeDeleted             */
+    int32_t pad_;
+} cb_attempt_view;
+
+typedef struct cb_context cb_context;
+
+/* Last error message of the calling thread ("" if none). */
+CB_API const char *cb_last_error(void);
+
+/* Allocates the device state for cfg->capacity bubbles on the current CUDA
+ * device. Replaces init()'s allocation and constant upload
+ * (src/simulator.cu:608-671). */
+CB_API int cb_create(const cb_config *cfg, cb_context **out);
+/* Frees everything. Replaces end() (src/simulator.cu:514-525). */
+CB_API int cb_destroy(cb_context *ctx);
+
+/* Uploads / downloads the persistent state (host buffers, `count` rows). */
+CB_API int cb_load_state(cb_context *ctx, const cb_state_view *state);
+CB_API int cb_get_state(cb_context *ctx, cb_state_view *state);
+
+/* Switches the integration options, as stabilize() does
+ * (src/simulator.cu:339-360) and simulate() does (:996-1003). */
+CB_API int cb_set_options(cb_context *ctx, int32_t use_gas_exchange,
+                   int32_t use_flow, int32_t increment_path);
+/* Sets dt (HostData.timeStep) and the time accumulator. */
+CB_API int cb_set_time(cb_context *ctx, double time_step, uint64_t time_integer,
+                double time_fraction);
+/* Replaces the device copy of the box and volume-fix constants after the box
+ * rescale of init() (src/simulator.cu:793-833). */
+CB_API int cb_set_box(cb_context *ctx, const double lbb[3], const double tfr[3],
+               double bubble_volume_multiplier, const double flow_lbb[3],
+               const double flow_tfr[3]);
+
+/* Euler bootstrap of the Adams-Bashforth history
+ * (src/simulator.cu:727-787): dxdto := F(x + dt F(x)), drdto := 0,
+ * path := 0. Needs a pair list. */
+CB_API int cb_bootstrap(cb_context *ctx);
+
+/* searchNeighbors() (src/simulator.cu:60-178): wrap, cell sort of all rows,
+ * saved := positions, pair list, neighbour counts. */
+CB_API int cb_search_neighbors(cb_context *ctx);
+/* Copies the pair list (Pairs, src/data_definitions.h:157-178). */
+CB_API int cb_get_pairs(cb_context *ctx, int32_t *i, int32_t *j, int32_t capacity,
+                 int32_t *count);
+/* Replaces the pair list (for harnesses that feed a list made elsewhere). */
+CB_API int cb_set_pairs(cb_context *ctx, const int32_t *i, const int32_t *j,
+                 int32_t count);
+
+/* One step() attempt without accepting it (src/simulator.cu:192-249):
+ * predict, pairwise interaction, correct; dt is then updated as step() does.
+ * The state stays at the start of the step. */
+CB_API int cb_attempt(cb_context *ctx, cb_attempt_view *out);
+
+/* n_steps calls of integrate() (src/simulator.cu:251-337): the reject loop,
+ * buffer rotation, time accumulation, removeBubbles() when bubbles fall
+ * below min_rad, and searchNeighbors() at half the skin. */
+CB_API int cb_integrate(cb_context *ctx, int64_t n_steps, cb_report *report);
+/* As cb_integrate, and returns the device time of the call measured with
+ * CUDA events on the context's stream. */
+CB_API int cb_integrate_timed(cb_context *ctx, int64_t n_steps, cb_report *report,
+                       double *device_ms);
+CB_API int cb_get_report(cb_context *ctx, cb_report *report);
+
+/* totalEnergy() (src/simulator.cu:39-58, kernel src/kernels.cu:941-957). */
+CB_API int cb_energy(cb_context *ctx, double *energy);
+/* Per-bubble energies (saveSnapshot's energy column, src/simulator.cu:389-392). */
+CB_API int cb_bubble_energies(cb_context *ctx, double *energy, int32_t capacity);
+/* totalVolume() (src/simulator.cu:362-379, kernel src/kernels.cu:1013-1024). */
+CB_API int cb_total_volume(cb_context *ctx, double *volume);
+
+/* Measurement: runs `reps` step() attempts without accepting them and
+ * returns the mean device time in milliseconds of each of the three attempt
+ * kernels (ms[0] predict, ms[1] pairwise interaction, ms[2] correct),
+ * measured with CUDA events on the context's stream. */
+CB_API int cb_profile_kernels(cb_context *ctx, int32_t reps, double ms[3]);
+
+/* Number of kernels this library launched on the context so far (graph
+ * kernel nodes are counted per execution). */
+CB_API int cb_launch_count(cb_context *ctx, int64_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUBBLE_GB300_H */

@@ -1,0 +1,189 @@
+"""GPU parity: the CUDA path (through the C ABI) against the FP64 oracle on
+the same seeded inputs.
+
+Bars (FP64 form):
+  * cell order, permutation, pair lists, deletion / compaction order and all
+    integer rows: bit-exact;
+  * one attempt (velocities, radius rates, corrected positions, errors,
+    overlap areas, the global sums): max |gpu - oracle| <= 1e-12 max |oracle|
+    per row (FP64 atomics reorder the per-bubble sums);
+  * short trajectories (<= 30 accepted steps): 1e-9 of the row maximum, same
+    step / attempt / search / deletion counts.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import cubble_gb300 as cb
+from cubble_gb300 import workloads
+from cubble_gb300.foam import CubbleError
+from helpers import DROWS, IROWS, assert_rows_close, brute_pairs, by_index, max_rel, pair_set
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "2d": dict(n=3000, dim=2, phi=0.9, seed=101),
+    "3d": dict(n=3000, dim=3, phi=0.8, seed=102, rstd=0.15, rclip=(0.3, 2.5)),
+    "2d-wallx": dict(n=2000, dim=2, phi=0.85, seed=103, wall=(1, 0, 0), wall_drag=0.2),
+    "3d-wallz": dict(n=2000, dim=3, phi=0.8, seed=104, wall=(0, 0, 1), wall_drag=0.1),
+    "2d-small": dict(n=12, dim=2, phi=0.9, seed=105),
+    "3d-small": dict(n=40, dim=3, phi=0.8, seed=106),
+}
+
+
+def make(case, **over):
+    c = dict(CASES[case])
+    c.update(over)
+    n, dim, phi = c.pop("n"), c.pop("dim"), c.pop("phi")
+    return workloads.foam(n, dim, phi, **c)
+
+
+def pair_both(oracle_mod, cfg, st):
+    g = cb.GpuFoam(cfg)
+    o = oracle_mod.OracleFoam(cfg)
+    g.load_state(st)
+    o.load_state(st)
+    return g, o
+
+
+def int_rows_equal(a, b):
+    for k in IROWS:
+        assert np.array_equal(a[k], b[k]), k
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_search_bit_exact(oracle_mod, case):
+    cfg, st = make(case)
+    g, o = pair_both(oracle_mod, cfg, st)
+    g.search_neighbors()
+    o.search_neighbors()
+    sg, so = g.get_state(), o.get_state()
+    for k in DROWS:
+        assert np.array_equal(sg[k], so[k]), k
+    int_rows_equal(sg, so)
+    gi, gj = g.pairs()
+    oi, oj = o.pairs()
+    assert np.array_equal(gi, oi) and np.array_equal(gj, oj)
+    assert set(zip(gi.tolist(), gj.tolist())) == brute_pairs(cfg, sg)
+
+
+@pytest.mark.parametrize("case", ["2d", "3d", "2d-wallx", "3d-wallz"])
+def test_bootstrap_and_attempt(oracle_mod, case):
+    cfg, st = make(case)
+    g, o = pair_both(oracle_mod, cfg, st)
+    for f in (g, o):
+        workloads.prepare(f)
+    sg, so = g.get_state(), o.get_state()
+    assert_rows_close(sg, so, ["dxdto", "dydto", "dzdto"], 1e-12, "bootstrap ")
+    ag, ao = g.attempt(), o.attempt()
+    rows = ["xp", "yp", "zp", "rp", "dxdtp", "dydtp", "dzdtp", "drdtp", "error",
+            "path_new", "overlap"]
+    assert_rows_close(ag, ao, rows, 1e-12, "attempt ")
+    for k in ("total_area", "total_area_per_radius", "total_overlap_area",
+              "total_overlap_area_per_radius", "total_volume_new", "max_error",
+              "max_radius", "max_expansion"):
+        assert ag[k] == pytest.approx(ao[k], rel=1e-12, abs=1e-300), k
+    assert np.array_equal(ag["delete_flags"], ao["delete_flags"])
+    assert ag["num_to_be_deleted"] == ao["num_to_be_deleted"]
+    assert g.report()["time_step"] == o.report()["time_step"]
+
+
+def test_flow_attempt(oracle_mod):
+    cfg, st = make("2d", use_flow=1, flow_lbb=(0.0, 20.0, 0.0), flow_tfr=(30.0, 40.0, 0.0),
+                   flow_vel=(0.01, 0.0, 0.0))
+    g, o = pair_both(oracle_mod, cfg, st)
+    for f in (g, o):
+        workloads.prepare(f)
+        f.integrate(3)
+    ag, ao = g.attempt(), o.attempt()
+    assert_rows_close(ag, ao, ["xp", "yp", "dxdtp", "dydtp", "drdtp"], 1e-11, "flow ")
+
+
+@pytest.mark.parametrize("graph", [0, 1])
+@pytest.mark.parametrize("case", ["2d", "3d", "3d-wallz"])
+def test_trajectory(oracle_mod, case, graph):
+    cfg, st = make(case, use_graph=graph)
+    g, o = pair_both(oracle_mod, cfg, st)
+    for f in (g, o):
+        workloads.prepare(f)
+    rg = g.integrate(30)
+    ro = o.integrate(30)
+    for k in ("steps", "attempts", "searches", "deleted", "count", "num_pairs"):
+        assert rg[k] == ro[k], k
+    assert rg["time_step"] == pytest.approx(ro["time_step"], rel=1e-12)
+    sg, so = by_index(g.get_state()), by_index(o.get_state())
+    assert_rows_close(sg, so, ["x", "y", "z", "r", "dxdt", "dydt", "drdt", "path",
+                               "dxdto", "error"], 1e-9, "trajectory ")
+
+
+@pytest.mark.parametrize("graph", [0, 1])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_deletion_bit_exact_order(oracle_mod, dim, graph):
+    cfg, st = workloads.foam(3000, dim, 0.85, rstd=0.3, rclip=(0.01, 2.0), seed=110 + dim,
+                             min_rad=0.2, use_graph=graph)
+    g, o = pair_both(oracle_mod, cfg, st)
+    for f in (g, o):
+        workloads.prepare(f)
+    rg, ro = g.integrate(1), o.integrate(1)
+    assert ro["deleted"] > 0
+    for k in ("deleted", "count", "num_pairs", "searches"):
+        assert rg[k] == ro[k], k
+    sg, so = g.get_state(), o.get_state()
+    int_rows_equal(sg, so)
+    assert_rows_close(sg, so, ["x", "y", "z", "r", "dxdt", "drdt", "saved_r"], 1e-12, "delete ")
+    gi, gj = g.pairs()
+    oi, oj = o.pairs()
+    if rg["searches"] == 1:  # no re-search: compaction order itself
+        assert np.array_equal(gi, oi) and np.array_equal(gj, oj)
+    assert pair_set(gi, gj, sg["index"]) == pair_set(oi, oj, so["index"])
+    M = cfg.bubble_volume_multiplier
+    target = math.pi * M ** 2 if dim == 2 else 4.0 / 3.0 * math.pi * M ** 3
+    assert g.total_volume() == pytest.approx(target, rel=1e-12)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_energy_volume(oracle_mod, dim):
+    cfg, st = make("2d" if dim == 2 else "3d")
+    g, o = pair_both(oracle_mod, cfg, st)
+    for f in (g, o):
+        f.search_neighbors()
+    assert g.energy() == pytest.approx(o.energy(), rel=1e-12)
+    assert g.total_volume() == pytest.approx(o.total_volume(), rel=1e-12)
+    assert max_rel(g.bubble_energies(), o.bubble_energies()) <= 1e-12
+
+
+def test_graph_matches_eager(oracle_mod):
+    cfg0, st = make("3d", use_graph=0)
+    cfg1, _ = make("3d", use_graph=1)
+    a, b = cb.GpuFoam(cfg0), cb.GpuFoam(cfg1)
+    for f in (a, b):
+        f.load_state(st)
+        workloads.prepare(f)
+    ra, rb = a.integrate(40), b.integrate(40)
+    for k in ("steps", "attempts", "searches", "deleted", "count"):
+        assert ra[k] == rb[k], k
+    sa, sb = by_index(a.get_state()), by_index(b.get_state())
+    assert_rows_close(sa, sb, ["x", "y", "z", "r"], 1e-10, "graph ")
+    assert b.launch_count() > 0
+
+
+def test_pair_capacity_error(oracle_mod):
+    cfg, st = make("2d", pair_capacity=100)
+    g = cb.GpuFoam(cfg)
+    g.load_state(st)
+    with pytest.raises(CubbleError) as e:
+        g.search_neighbors()
+    assert e.value.code == 3
+
+
+@pytest.mark.parametrize("graph", [0, 1])
+def test_reject_loop_cap(oracle_mod, graph):
+    cfg, st = make("2d", tol=1e-30, max_attempts=5, use_graph=graph)
+    g = cb.GpuFoam(cfg)
+    g.load_state(st)
+    workloads.prepare(g)
+    with pytest.raises(CubbleError) as e:
+        g.integrate(1)
+    assert e.value.code == 4
+    assert g.report()["attempts"] == 5
