@@ -48,6 +48,10 @@ constexpr int kKernelsPerSearch = 15;
 
 }  // namespace
 
+namespace cbg {
+void set_last_error(const std::string &msg) { g_err = msg; }
+}  // namespace cbg
+
 struct cb_context {
     cb_config cfg{};
     int dev = 0, sms = 0;

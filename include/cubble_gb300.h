@@ -212,6 +212,35 @@ CB_API int cb_profile_kernels(cb_context *ctx, int32_t reps, double ms[3]);
  * kernel nodes are counted per execution). */
 CB_API int cb_launch_count(cb_context *ctx, int64_t *count);
 
+/* Total potential energy of a foam, as cb_energy computes it, for callers
+ * that cannot allocate device memory. No counterpart in the reference.
+ *
+ * Who needs it: applications whose device memory is owned by their own pool
+ * or arena, or code calling from a loop where cudaMalloc would synchronise
+ * the device or is not allowed. Such a caller owns the inputs and the
+ * output; this call allocates nothing (no cudaMalloc / cudaFree, no library
+ * allocator). Its scratch is one static device array inside the library,
+ * sized for at most 262,144 bubbles (about 2 MiB), which every GPU that
+ * loads the library holds until the process exits.
+ *
+ * x, y, z (3D only), r: `count` device rows; pair_i, pair_j: `num_pairs`
+ * device rows of bubble indices; energy_out: one device double that
+ * receives sum_i sum_{pairs of i} (r_i + r_j - |d_ij|)^2 over overlapping
+ * pairs. Only dimensionality, wall[] and the box corners of `cfg` are read.
+ * `stream` is a cudaStream_t (NULL = the default stream); the work is
+ * enqueued there and the call returns without waiting.
+ *
+ * count > 262,144 is rejected with CB_ERR_CAPACITY before any GPU work.
+ * The first call on a device looks up the device address of the static
+ * array with that device current; make that first call before any stream
+ * capture. Every call reuses the same array and clears what must start at
+ * zero, so calls that overlap on the GPU (different streams, or several
+ * host threads) race with each other: serialise them. */
+CB_API int cb_energy_noalloc(const cb_config *cfg, const double *x, const double *y,
+                             const double *z, const double *r, const int32_t *pair_i,
+                             const int32_t *pair_j, int32_t count, int32_t num_pairs,
+                             double *energy_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
