@@ -64,6 +64,7 @@ struct DevConst {
     double lbb[3], tfr[3], iv[3];
     double flow_lbb[3], flow_tfr[3], flow_vel[3];
     double wall_drag, min_rad, f0, K, kappa, skin, vol_mul_const, ain, tol;
+    double half_iv[3];
     float pre_margin;  // FP32 pair-search prefilter margin (length units)
     float half_iv32[3];
     float iv32[3];
@@ -207,6 +208,53 @@ __device__ __forceinline__ double fold_partials(const double *p, int nblocks, bo
         v = is_max ? fmax(v, t) : v + t;
     }
     return is_max ? block_reduce(v, OpMax(), smem) : block_reduce(v, OpSum(), smem);
+}
+
+// ---------------------------------------------------------- FP64 helpers
+// GB300 issues 2 FP64 thread-instructions per SM and cycle (1/64 of FP32),
+// so the FP64 kernels avoid the multi-instruction IEEE divide and square
+// root where full IEEE rounding is not needed.
+//
+// Reciprocal and reciprocal square root: the hardware's approximate FP64
+// estimate y0 (PTX rcp.approx.ftz.f64 / rsqrt.approx.f64, ~2^-22 relative)
+// refined by one third-order Householder (Newton-Raphson with the second
+// order term) correction. With e = 1 - a y0 (resp. 1 - a y0^2):
+//   1/a       = y0 (1 + e + e^2 + ...)            -> error ~ e^3
+//   1/sqrt(a) = y0 (1 + e/2 + 3 e^2 / 8 + ...)    -> error ~ 5/16 e^3
+// i.e. a few ulp, for positive normal arguments. 3 and 5 FP64 instructions.
+__device__ __forceinline__ double rcp_hn(double a) {
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(a));
+    const double e = fma(-a, y, 1.0);
+    return fma(y, fma(e, e, e), y);
+}
+__device__ __forceinline__ double rsqrt_hn(double a) {
+    double y;
+    asm("rsqrt.approx.f64 %0, %1;" : "=d"(y) : "d"(a));
+    const double t = a * y;
+    const double e = fma(-t, y, 1.0);
+    return fma(y * e, fma(e, 0.375, 0.5), y);
+}
+// sqrt(a) = a / sqrt(a) for a > 0, 0 for a <= 0.
+__device__ __forceinline__ double sqrt_hn(double a) { return a > 0.0 ? a * rsqrt_hn(a) : 0.0; }
+
+// Minimum image on a periodic axis: |d| > L/2 is tested on the bit patterns
+// (non-negative doubles order like their bits), so the test costs no FP64
+// instruction; d - sign(d) L equals the reference's (L - |d|) (+-1).
+__device__ __forceinline__ double min_image(double d, double half_iv, double iv) {
+    const long long ad = __double_as_longlong(d) & 0x7fffffffffffffffLL;
+    if (ad > __double_as_longlong(half_iv)) d = d - copysign(iv, d);
+    return d;
+}
+
+// Running maximum of doubles >= 0 (or any double against a running maximum
+// that starts at 0) on the integer pipe: for x >= 0 the signed 64-bit
+// pattern orders like the value, and negative values lose against 0.
+__device__ __forceinline__ long long max_bits(long long m, double x) {
+    return max(m, __double_as_longlong(x));
+}
+__device__ __forceinline__ bool finite_bits(double x) {
+    return (__double_as_longlong(x) & 0x7ff0000000000000LL) != 0x7ff0000000000000LL;
 }
 
 // wrappedDifference, src/kernels.cu:1094-1114 (minimum image on periodic axes)

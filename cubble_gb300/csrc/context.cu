@@ -140,6 +140,7 @@ void fill_const(cb_context *c) {
     for (int a = 0; a < 3; a++) {
         maxabs = std::max(maxabs, std::max(std::fabs(k.lbb[a]), std::fabs(k.tfr[a])));
         maxiv = std::max(maxiv, k.iv[a]);
+        k.half_iv[a] = 0.5 * k.iv[a];
         k.half_iv32[a] = (float)(0.5 * k.iv[a]);
         k.iv32[a] = (float)k.iv[a];
     }

@@ -240,127 +240,146 @@ __global__ void __launch_bounds__(kBlock) k_permute_b(Bufs b) {
     }
 }
 
-// Unique neighbour cells of `cell` with linear index >= cell, ascending.
+// Neighbour cell `k` (0..26, offsets dx,dy,dz in -1..1) of `cell`, or
+// INT_MAX when it is below `cell` in linear order, outside a wall, on an
+// unused axis, or a duplicate of another offset on a periodic axis with
+// fewer than three cells (one cell: offset 0 only; two: 0 and +1).
 template <int DIM>
-__device__ __forceinline__ int upper_cells(const DevConst &k, const int cd[3], int cell,
-                                           int out[27]) {
-    const int kx = cell % cd[0], ky = (cell / cd[0]) % cd[1], kz = cell / (cd[0] * cd[1]);
-    int nxs[3], nys[3], nzs[3];
-    int mx = 0, my = 0, mz = 0;
-    const int kk[3] = {kx, ky, kz};
-    int *outs[3] = {nxs, nys, nzs};
-    int *ms[3] = {&mx, &my, &mz};
+__device__ __forceinline__ int neighbor_cell(const DevConst &k, const int cd[3], int cell, int o) {
+    const int off[3] = {o % 3 - 1, (o / 3) % 3 - 1, o / 9 - 1};
+    const int kk[3] = {cell % cd[0], (cell / cd[0]) % cd[1], cell / (cd[0] * cd[1])};
+    int q[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        int *o = outs[a];
-        int &m = *ms[a];
-        const int q = kk[a], d = cd[a];
+        const int d = cd[a];
         if (a >= DIM) {
-            o[m++] = 0;
+            if (off[a] != 0) return 0x7fffffff;
+            q[a] = 0;
         } else if (!k.wall[a]) {
-            if (d == 1) {
-                o[m++] = q;
-            } else if (d == 2) {
-                o[m++] = q;
-                o[m++] = (q + 1) % 2;
-            } else {
-                o[m++] = (q + d - 1) % d;
-                o[m++] = q;
-                o[m++] = (q + 1) % d;
-            }
+            if (d == 1 && off[a] != 0) return 0x7fffffff;
+            if (d == 2 && off[a] == -1) return 0x7fffffff;
+            q[a] = (kk[a] + off[a] + d) % d;
         } else {
-            for (int t = -1; t <= 1; t++)
-                if (q + t >= 0 && q + t < d) o[m++] = q + t;
+            q[a] = kk[a] + off[a];
+            if (q[a] < 0 || q[a] >= d) return 0x7fffffff;
         }
     }
-    int m = 0;
-    for (int az = 0; az < mz; az++)
-        for (int ay = 0; ay < my; ay++)
-            for (int ax = 0; ax < mx; ax++) {
-                const int v = (nzs[az] * cd[1] + nys[ay]) * cd[0] + nxs[ax];
-                if (v < cell) continue;
-                int p = m++;
-                while (p > 0 && out[p - 1] > v) {
-                    out[p] = out[p - 1];
-                    p--;
-                }
-                out[p] = v;
-            }
-    return m;
+    const int v = (q[2] * cd[1] + q[1]) * cd[0] + q[0];
+    return v >= cell ? v : 0x7fffffff;
 }
 
-// Pair rows of bubble i. WRITE=false counts, WRITE=true writes at `base`.
+// Warp-wide ascending bitonic sort of one int per lane.
+__device__ __forceinline__ int warp_sort(int v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int size = 2; size <= 32; size <<= 1) {
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            const int o = __shfl_xor_sync(0xffffffffu, v, stride);
+            const bool up = ((lane & size) == 0);
+            const bool lower = ((lane & stride) == 0);
+            v = (lower == up) ? min(v, o) : max(v, o);
+        }
+    }
+    return v;
+}
+
+constexpr int kWarpsPerBlock = kBlock / 32;
+
+// Pair rows of one cell per warp: lanes are the cell's bubbles (32 at a
+// time); each neighbour cell with a linear index >= the home cell is staged
+// 32 bubbles at a time in shared memory (FP32 x, y, z, r) and every lane
+// tests its bubble against the staged ones. A candidate is decided in FP32
+// unless its distance lies within the guard band `pre_margin` of the cutoff;
+// only there the exact FP64 test of comparePair (src/kernels.cu:619-623)
+// runs, so the pair set equals the FP64 one bit for bit.
+// WRITE = false counts rows, WRITE = true writes them at rowStart.
 template <int DIM, bool WRITE>
-__device__ __forceinline__ int pair_row(const Bufs &b, const DevConst &k, const Ctrl *c, int i,
-                                        const double *X, const double *Y, const double *Z,
-                                        const double *R, int *PI, int *PJ, int base, int pcap) {
-    const int cd[3] = {c->cell_dims[0], c->cell_dims[1], c->cell_dims[2]};
-    const int cell = b.cellSorted[i];
-    int cells[27];
-    const int m = upper_cells<DIM>(k, cd, cell, cells);
-    const float4 pi = b.pos32[i];
-    const float skin32 = (float)k.skin + k.pre_margin;
-    const bool per[3] = {!k.wall[0], !k.wall[1], !k.wall[2]};
-    int cnt = 0;
-    for (int qi = 0; qi < m; qi++) {
-        const int q = cells[qi];
-        int s = b.cellStart[q];
-        const int e = b.cellStart[q + 1];
-        if (q == cell) s = i + 1;
-        for (int j = s; j < e; j++) {
-            const float4 pj = b.pos32[j];
-            float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-            if (per[0] && fabsf(dx) > k.half_iv32[0]) dx = fabsf(dx) - k.iv32[0];
-            if (per[1] && fabsf(dy) > k.half_iv32[1]) dy = fabsf(dy) - k.iv32[1];
-            if (DIM == 3 && per[2] && fabsf(dz) > k.half_iv32[2]) dz = fabsf(dz) - k.iv32[2];
-            const float cut = pi.w + pj.w + skin32;
-            float d2 = dx * dx + dy * dy;
-            if (DIM == 3) d2 += dz * dz;
-            if (d2 >= cut * cut) continue;
-            // exact test of comparePair, src/kernels.cu:619-623
-            const double maxd = __dadd_rn(__dadd_rn(R[i], R[j]), k.skin);
-            const double sq = exact_sqdist<DIM>(k, X[i], Y[i], DIM == 3 ? Z[i] : 0.0, X[j], Y[j],
-                                                DIM == 3 ? Z[j] : 0.0);
-            if (sq < __dmul_rn(maxd, maxd)) {
-                if (WRITE && base + cnt < pcap) {
-                    PI[base + cnt] = i;
-                    PJ[base + cnt] = j;
-                }
-                cnt++;
-            }
-        }
-    }
-    return cnt;
-}
-
-template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_pair_count(Bufs b) {
-    const Ctrl *c = b.ctrl;
-    const DevConst &k = *b.k;
-    const int n = c->n;
-    const double *X = drow(b, c, RX), *Y = drow(b, c, RY), *Z = drow(b, c, RZ),
-                 *R = drow(b, c, RR);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        b.rowCount[i] = pair_row<DIM, false>(b, k, c, i, X, Y, Z, R, nullptr, nullptr, 0, 0);
-}
-
-template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_pair_fill(Bufs b) {
+__global__ void __launch_bounds__(kBlock) k_pair_cells(Bufs b) {
+    __shared__ float4 stage[kWarpsPerBlock][32];
     Ctrl *c = b.ctrl;
     const DevConst &k = *b.k;
-    const int n = c->n;
+    const int ncell = c->ncell;
+    const int cd[3] = {c->cell_dims[0], c->cell_dims[1], c->cell_dims[2]};
     const double *X = drow(b, c, RX), *Y = drow(b, c, RY), *Z = drow(b, c, RZ),
                  *R = drow(b, c, RR);
     int *PI = b.ps[c->prole[PI0]];
     int *PJ = b.ps[c->prole[PJ0]];
     int *NN = irow(b, c, INN);
     const int pcap = k.pcap;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int cnt = b.rowCount[i];
-        NN[i] = cnt;
-        if (cnt) pair_row<DIM, true>(b, k, c, i, X, Y, Z, R, PI, PJ, b.rowStart[i], pcap);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const float skin32 = (float)k.skin, band = k.pre_margin;
+    const bool per[3] = {!k.wall[0], !k.wall[1], !k.wall[2]};
+    const int warps = gridDim.x * kWarpsPerBlock;
+    for (int cell = blockIdx.x * kWarpsPerBlock + w; cell < ncell; cell += warps) {
+        const int s0 = b.cellStart[cell], e0 = b.cellStart[cell + 1];
+        if (s0 == e0) continue;
+        const int nbr = warp_sort(lane < 27 ? neighbor_cell<DIM>(k, cd, cell, lane) : 0x7fffffff);
+        const int m = __popc(__ballot_sync(0xffffffffu, nbr != 0x7fffffff));
+        for (int h0 = s0; h0 < e0; h0 += 32) {
+            const int i = h0 + lane;
+            const bool active = i < e0;
+            float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
+            double xi = 0.0, yi = 0.0, zi = 0.0, ri = 0.0;
+            int base = 0, cnt = 0;
+            if (active) {
+                pi = b.pos32[i];
+                if (WRITE) base = b.rowStart[i];
+            }
+            for (int qn = 0; qn < m; qn++) {
+                const int q = __shfl_sync(0xffffffffu, nbr, qn);
+                const int cs = b.cellStart[q], ce = b.cellStart[q + 1];
+                for (int c0 = cs; c0 < ce; c0 += 32) {
+                    const int nc = min(32, ce - c0);
+                    __syncwarp();
+                    if (lane < nc) stage[w][lane] = b.pos32[c0 + lane];
+                    __syncwarp();
+                    for (int t = 0; t < nc; t++) {
+                        const int j = c0 + t;
+                        const float4 pj = stage[w][t];
+                        if (!active || j <= i) continue;
+                        float dx = fabsf(pi.x - pj.x), dy = fabsf(pi.y - pj.y);
+                        float dz = DIM == 3 ? fabsf(pi.z - pj.z) : 0.f;
+                        if (per[0] && dx > k.half_iv32[0]) dx = k.iv32[0] - dx;
+                        if (per[1] && dy > k.half_iv32[1]) dy = k.iv32[1] - dy;
+                        if (DIM == 3 && per[2] && dz > k.half_iv32[2]) dz = k.iv32[2] - dz;
+                        float d2 = fmaf(dx, dx, dy * dy);
+                        if (DIM == 3) d2 = fmaf(dz, dz, d2);
+                        const float cut = pi.w + pj.w + skin32;
+                        const float hi = cut + band, lo = fmaxf(cut - band, 0.f);
+                        if (d2 >= hi * hi) continue;
+                        bool take = d2 < lo * lo;
+                        if (!take) {
+                            if (ri == 0.0) {
+                                xi = X[i];
+                                yi = Y[i];
+                                zi = DIM == 3 ? Z[i] : 0.0;
+                                ri = R[i];
+                            }
+                            const double maxd = __dadd_rn(__dadd_rn(ri, R[j]), k.skin);
+                            const double sq = exact_sqdist<DIM>(k, xi, yi, zi, X[j], Y[j],
+                                                                DIM == 3 ? Z[j] : 0.0);
+                            take = sq < __dmul_rn(maxd, maxd);
+                        }
+                        if (take) {
+                            if (WRITE && base + cnt < pcap) {
+                                PI[base + cnt] = i;
+                                PJ[base + cnt] = j;
+                            }
+                            cnt++;
+                        }
+                    }
+                }
+            }
+            if (active) {
+                if (WRITE)
+                    NN[i] = cnt;
+                else
+                    b.rowCount[i] = cnt;
+            }
+        }
     }
-    if (last_block(&c->done[DC_MISC]) && threadIdx.x == 0) {
+    if (WRITE && last_block(&c->done[DC_MISC]) && threadIdx.x == 0) {
         const int found = c->np_found;
         if (found > pcap) {
             c->status = CB_ERR_CAPACITY;
@@ -403,18 +422,18 @@ void launch_search(const Launch &l, const Bufs &b, int dim) {
     if (dim == 3) {
         k_permute_a<3><<<G, kBlock, 0, s>>>(b);
         k_permute_b<3><<<G, kBlock, 0, s>>>(b);
-        k_pair_count<3><<<G, kBlock, 0, s>>>(b);
+        k_pair_cells<3, false><<<G, kBlock, 0, s>>>(b);
     } else {
         k_permute_a<2><<<G, kBlock, 0, s>>>(b);
         k_permute_b<2><<<G, kBlock, 0, s>>>(b);
-        k_pair_count<2><<<G, kBlock, 0, s>>>(b);
+        k_pair_cells<2, false><<<G, kBlock, 0, s>>>(b);
     }
     *l.launches += 3;
     launch_scan(l, b, b.rowCount, b.rowStart, &c->n, 0, &c->np_found);
     if (dim == 3)
-        k_pair_fill<3><<<G, kBlock, 0, s>>>(b);
+        k_pair_cells<3, true><<<G, kBlock, 0, s>>>(b);
     else
-        k_pair_fill<2><<<G, kBlock, 0, s>>>(b);
+        k_pair_cells<2, true><<<G, kBlock, 0, s>>>(b);
     k_degree<<<G, kBlock, 0, s>>>(b);
     *l.launches += 2;
 }

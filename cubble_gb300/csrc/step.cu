@@ -33,13 +33,83 @@ __device__ __forceinline__ double4_32a ld4(const double *p, int i) {
     return reinterpret_cast<const double4_32a *>(p)[i];
 }
 
+// step(): accept / reject and the new dt (src/simulator.cu:239-246); on
+// accept, integrate()'s rotation and clock (src/simulator.cu:258-314) and the
+// delete / search decisions (:316-334). Run by one thread of the last block.
+template <int DIM>
+__device__ void finish_attempt(Ctrl *c, const DevConst &k, double fErr, double fRad,
+                               double fExp, double fVol, double fDel, double fBad) {
+    const int gas = c->use_gas, path = c->inc_path;
+    const int n = c->n;
+    c->done[DC_CORRECT] = 0;
+    c->max_err = fErr;
+    c->max_rad = fRad;
+    c->max_exp = fExp;
+    c->vol_new = fVol;
+    c->ndel = gas ? (int)fDel : 0;
+    c->attempts += 1;
+    c->attempts_this_step += 1;
+    const double tol = k.tol;
+    const int too_large = fErr > tol;
+    const int increase = fErr < 0.45 * tol && c->dt < 10;
+    if (too_large)
+        c->dt *= 0.37;
+    else if (increase)
+        c->dt *= 1.269;
+    c->too_large = too_large;
+    if (fBad > 0.0 || isnan(fErr)) c->status = CB_ERR_NONFINITE;
+    c->need_delete = 0;
+    c->need_search = 0;
+    if (too_large && c->status == CB_OK) {
+        if (c->attempts_this_step >= k.max_attempts) c->status = CB_ERR_MAX_ATTEMPTS;
+        if (c->dt < 1e-300) c->status = CB_ERR_DT_UNDERFLOW;
+    }
+    if (!too_large && !c->no_accept && c->status == CB_OK) {
+        int *r = c->drole;
+        for (int a = 0; a < DIM; a++) {
+            swap_role(r, RX + a, RXN + a);
+            const int old = r[RVO0 + a];
+            r[RVO0 + a] = r[RV0 + a];
+            r[RV0 + a] = r[RVP0 + a];
+            r[RVP0 + a] = old;
+        }
+        if (gas) {
+            swap_role(r, RR, RRN);
+            const int old = r[RVO3];
+            r[RVO3] = r[RV3];
+            r[RV3] = r[RVP3];
+            r[RVP3] = old;
+        }
+        if (path) swap_role(r, RPATH, RPATHN);
+        c->steps += 1;
+        c->bubble_steps += n;
+        c->attempts_this_step = 0;
+        // time accumulator, src/simulator.cu:311-314 (adds the updated dt)
+        c->tfrac += c->dt;
+        c->tint += (unsigned long long)c->tfrac;
+        c->tfrac = c->tfrac - (double)(unsigned long long)c->tfrac;
+        if (gas) {
+            c->max_bubble_radius = fRad;
+            c->need_delete = c->ndel > 0;
+        }
+        c->need_search = fExp >= 0.5 * k.skin;
+    }
+    if (c->graph_mode) {
+        const int ok = c->status == CB_OK;
+        const int accepted = !too_large;
+        set_cond(c->h_delete, ok && accepted && c->need_delete);
+        set_cond(c->h_search, ok && accepted && c->need_search);
+        set_cond(c->h_loop, ok && (too_large || c->steps < c->steps_target));
+    }
+}
+
 // ---------------------------------------------------------------- predict
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_predict(Bufs b) {
     __shared__ double smem[32];
     const Ctrl *c = b.ctrl;
     const int n = c->n;
-    const double ts = c->dt;
+    const double h = 0.5 * c->dt;
     const int gas = c->use_gas;
     const double *X = drow(b, c, RX), *Y = drow(b, c, RY), *Z = drow(b, c, RZ),
                  *R = drow(b, c, RR);
@@ -50,16 +120,16 @@ __global__ void __launch_bounds__(kBlock) k_predict(Bufs b) {
     double sA = 0.0, sAr = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         // p + 0.5 ts (3 v - vo), src/kernels.cu:48-50
-        const double xp = X[i] + 0.5 * ts * (3.0 * V0[i] - O0[i]);
-        const double yp = Y[i] + 0.5 * ts * (3.0 * V1[i] - O1[i]);
+        const double xp = fma(h, fma(3.0, V0[i], -O0[i]), X[i]);
+        const double yp = fma(h, fma(3.0, V1[i], -O1[i]), Y[i]);
         double rp = R[i];
-        if (gas) rp = R[i] + 0.5 * ts * (3.0 * V3[i] - O3[i]);
-        const double inv = 1.0 / rp;
+        if (gas) rp = fma(h, fma(3.0, V3[i], -O3[i]), rp);
+        const double inv = rcp_hn(rp);
         double4_32a p;
         if (DIM == 3) {
             p.x = xp;
             p.y = yp;
-            p.z = Z[i] + 0.5 * ts * (3.0 * V2[i] - O2[i]);
+            p.z = fma(h, fma(3.0, V2[i], -O2[i]), Z[i]);
             p.w = rp;
             b.invr[i] = inv;
         } else {
@@ -70,9 +140,8 @@ __global__ void __launch_bounds__(kBlock) k_predict(Bufs b) {
         }
         reinterpret_cast<double4_32a *>(b.pred)[i] = p;
         if (gas) {  // area and area per radius, src/kernels.cu:103-112
-            double apr = 2.0 * kPi;
-            if (DIM == 3) apr *= 2.0 * rp;
-            sA += apr * rp;
+            const double apr = DIM == 3 ? (4.0 * kPi) * rp : 2.0 * kPi;
+            sA = fma(apr, rp, sA);
             sAr += apr;
         }
     }
@@ -95,7 +164,10 @@ __global__ void __launch_bounds__(kBlock) k_predict(Bufs b) {
 
 // ------------------------------------------------------------------ pairs
 // One lane per pair; contributions to both members go through FP64 atomics
-// into the per-bubble accumulator rows.
+// into the per-bubble accumulator rows. FP64-issue bound on GB300, so:
+// minimum image by bit compare, 1/sqrt(m) and 1/(r1 + r2) by rsqrt_hn /
+// rcp_hn, the division by m of the overlap formula as a product with
+// (1/sqrt(m))^2.
 template <int DIM, bool GAS, bool FLOW>
 __global__ void __launch_bounds__(kBlock) k_pairs(Bufs b) {
     __shared__ double smem[32];
@@ -106,6 +178,9 @@ __global__ void __launch_bounds__(kBlock) k_pairs(Bufs b) {
     const int *PJ = b.ps[c->prole[PJ0]];
     const double *V0 = drow(b, c, RV0), *V1 = drow(b, c, RV1), *V2 = drow(b, c, RV2);
     const double f0 = k.f0;
+    const bool px = !k.wall[0], py = !k.wall[1], pz = DIM == 3 && !k.wall[2];
+    const double hx = k.half_iv[0], hy = k.half_iv[1], hz = k.half_iv[2];
+    const double Lx = k.iv[0], Ly = k.iv[1], Lz = k.iv[2];
     double sAo = 0.0, sAor = 0.0;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
         const int i = PI[p], j = PJ[p];
@@ -117,27 +192,23 @@ __global__ void __launch_bounds__(kBlock) k_pairs(Bufs b) {
             if (DIM == 3) atomicAdd(aj + 7, V2[i]);
         }
         const double4_32a a = ld4(b.pred, i), q = ld4(b.pred, j);
-        double r1, r2, zi = 0.0, zj = 0.0, inv1, inv2;
+        const double r1 = DIM == 3 ? a.w : a.z, r2 = DIM == 3 ? q.w : q.z;
+        // wrappedDifference, src/kernels.cu:1094-1114
+        double dx = a.x - q.x, dy = a.y - q.y, dz = 0.0;
+        if (px) dx = min_image(dx, hx, Lx);
+        if (py) dy = min_image(dy, hy, Ly);
         if (DIM == 3) {
-            zi = a.z;
-            zj = q.z;
-            r1 = a.w;
-            r2 = q.w;
-            inv1 = inv2 = 0.0;
-        } else {
-            r1 = a.z;
-            r2 = q.z;
-            inv1 = a.w;
-            inv2 = q.w;
+            dz = a.z - q.z;
+            if (pz) dz = min_image(dz, hz, Lz);
         }
+        double m = dx * dx;
+        m = fma(dy, dy, m);
+        if (DIM == 3) m = fma(dz, dz, m);
         const double radii = r1 + r2;
-        double dx, dy, dz;
-        wrapped_diff<DIM>(k, a.x, a.y, zi, q.x, q.y, zj, dx, dy, dz);
-        double m = dx * dx + dy * dy;
-        if (DIM == 3) m += dz * dz;
-        if (radii * radii >= m) {
-            // velocity, src/kernels.cu:218-233
-            const double s = f0 * (rsqrt(m) - 1.0 / radii);
+        if (fma(radii, radii, -m) >= 0.0) {
+            // velocity f0 d (1/|d| - 1/(r1 + r2)), src/kernels.cu:218-233
+            const double rs = rsqrt_hn(m);
+            const double s = f0 * (rs - rcp_hn(radii));
             const double fx = dx * s, fy = dy * s;
             atomicAdd(ai + 0, fx);
             atomicAdd(aj + 0, -fx);
@@ -150,30 +221,33 @@ __global__ void __launch_bounds__(kBlock) k_pairs(Bufs b) {
             }
             if (GAS) {  // pairwise gas exchange, src/kernels.cu:236-280
                 const double r1sq = r1 * r1, r2sq = r2 * r2;
+                const bool inside = m < r1sq || m < r2sq;
                 double oa;
-                if (m < r1sq || m < r2sq) {
-                    oa = r1sq < r2sq ? r1sq : r2sq;
-                } else {
-                    oa = 0.5 * (r2sq - r1sq + m);
-                    oa *= oa;
-                    oa /= m;
-                    oa = r2sq - oa;
-                    oa = oa < 0 ? -oa : oa;
-                }
                 if (DIM == 3) {
+                    if (inside) {
+                        oa = fmin(r1sq, r2sq);
+                    } else {
+                        const double t = 0.5 * (r2sq - r1sq + m);
+                        oa = fabs(r2sq - (t * t) * (rs * rs));
+                    }
                     oa *= kPi;
-                    inv1 = b.invr[i];
-                    inv2 = b.invr[j];
                 } else {
-                    oa = 2.0 * sqrt(oa);
+                    if (inside) {
+                        oa = 2.0 * fmin(r1, r2);
+                    } else {
+                        const double t = 0.5 * (r2sq - r1sq + m);
+                        oa = 2.0 * sqrt_hn(fabs(r2sq - (t * t) * (rs * rs)));
+                    }
                 }
+                const double inv1 = DIM == 3 ? b.invr[i] : a.w;
+                const double inv2 = DIM == 3 ? b.invr[j] : q.w;
                 const double g = oa * (inv2 - inv1);
                 atomicAdd(ai + 3, g);
                 atomicAdd(aj + 3, -g);
                 atomicAdd(ai + 4, oa);
                 atomicAdd(aj + 4, oa);
-                sAo += 2.0 * oa;
-                sAor += oa * (inv1 + inv2);
+                sAo += oa;
+                sAor = fma(oa, inv1 + inv2, sAor);
             }
             if (FLOW) {  // src/kernels.cu:298-307 (overlapping pairs only)
                 atomicAdd(ai + 5, V0[j]);
@@ -192,7 +266,7 @@ __global__ void __launch_bounds__(kBlock) k_pairs(Bufs b) {
         const double fAo = fold_partials(b.part + 2 * gridDim.x, gridDim.x, false, smem);
         const double fAor = fold_partials(b.part + 3 * gridDim.x, gridDim.x, false, smem);
         if (threadIdx.x == 0) {
-            b.ctrl->sumAo = fAo;
+            b.ctrl->sumAo = 2.0 * fAo;  // each pair adds 2 A_overlap, :267
             b.ctrl->sumAor = fAor;
             b.ctrl->done[DC_PAIRS] = 0;
         }
@@ -223,6 +297,7 @@ __global__ void __launch_bounds__(kBlock) k_correct(Bufs b) {
     const DevConst &k = *b.k;
     const int n = c->n;
     const double ts = c->dt;
+    const double h = 0.5 * ts;
     const int gas = c->use_gas, flow = c->use_flow, path = c->inc_path;
     const double *X = drow(b, c, RX), *Y = drow(b, c, RY), *Z = drow(b, c, RZ),
                  *R = drow(b, c, RR);
@@ -237,12 +312,15 @@ __global__ void __launch_bounds__(kBlock) k_correct(Bufs b) {
     const double *PATH = drow(b, c, RPATH);
     double *PATHN = drow(b, c, RPATHN), *ERR = drow(b, c, RERR);
     const int *NN = irow(b, c, INN);
-    // mean-field factors, src/kernels.cu:399-404 (uniform over bubbles)
+    // mean-field factors, src/kernels.cu:399-408 (uniform over bubbles);
+    // area = 4 pi r^2 (3D) / 2 pi r (2D), so K / area = kq / r^2 (/ r)
     const double sA = c->sumA, sAr = c->sumAr, sAo = c->sumAo, sAor = c->sumAor;
     const double mfa = (sAr - sAor) / (sA - sAo);
     const double mfb = k.kappa * k.ain * (double)n / sA;
+    const double kq = DIM == 3 ? k.K / (4.0 * kPi) : k.K / (2.0 * kPi);
     const double drag = 1.0 - k.wall_drag;
-    double merr = 0.0, mrad = 0.0, mexp = 0.0, vol = 0.0;
+    long long merr = 0, mrad = 0, mexp = 0;
+    double vol = 0.0;
     int ndel = 0, bad = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         double *acc = b.acc + (size_t)i * kAcc;
@@ -295,66 +373,66 @@ __global__ void __launch_bounds__(kBlock) k_correct(Bufs b) {
                 vpz += velocity * xDrag * yDrag;
             }
         }
-        // AM2 correct, src/kernels.cu:487-495 and :366-387
-        double e = 0.0, dist = 0.0, t;
+        // AM2 correct x + 0.5 ts (v + vp), src/kernels.cu:487-495 and :366-387
+        long long e = 0;
+        double t, dist;
         const double x0 = X[i], y0 = Y[i];
-        const double cx = x0 + 0.5 * ts * (V0[i] + vpx);
-        e = fmax(e, fabs(xp - cx));
+        const double cx = fma(h, V0[i] + vpx, x0);
+        e = max_bits(e, fabs(xp - cx));
         t = cx - S0[i];
-        dist += t * t;
-        const double cy = y0 + 0.5 * ts * (V1[i] + vpy);
-        e = fmax(e, fabs(yp - cy));
+        dist = t * t;
+        const double cy = fma(h, V1[i] + vpy, y0);
+        e = max_bits(e, fabs(yp - cy));
         t = cy - S1[i];
-        dist += t * t;
+        dist = fma(t, t, dist);
         double cz = 0.0, z0 = 0.0;
         if (DIM == 3) {
             z0 = Z[i];
-            cz = z0 + 0.5 * ts * (V2[i] + vpz);
-            e = fmax(e, fabs(zp - cz));
+            cz = fma(h, V2[i] + vpz, z0);
+            e = max_bits(e, fabs(zp - cz));
             t = cz - S2[i];
-            dist += t * t;
+            dist = fma(t, t, dist);
         }
-        dist = sqrt(dist);
+        dist = sqrt_hn(dist);
         int del = 0;
         if (gas) {  // mean-field gas exchange and radius, src/kernels.cu:390-431
-            double area = 2.0 * kPi * rp;
-            if (DIM == 3) area *= 2.0 * rp;
-            double vr = mfa - 1.0 / rp;
+            const double inv = DIM == 3 ? b.invr[i] : p.w;
+            const double area = DIM == 3 ? (4.0 * kPi) * (rp * rp) : (2.0 * kPi) * rp;
+            double vr = mfa - inv;
             vr *= mfb * (area - ov);
             vr += vpr;
-            vr *= k.K / area;
+            vr *= DIM == 3 ? kq * (inv * inv) : kq * inv;
             vpr = vr;
-            const double cr = R[i] + 0.5 * ts * (V3[i] + vr);
-            e = fmax(e, fabs(rp - cr));
+            const double cr = fma(h, V3[i] + vr, R[i]);
+            e = max_bits(e, fabs(rp - cr));
             dist += cr - S3[i];
             if (cr > k.min_rad) {
-                double v3 = cr * cr;
-                if (DIM == 3) v3 *= cr;
-                vol += v3;
+                vol = fma(DIM == 3 ? cr * cr : cr, cr, vol);
             } else {
                 del = 1;
                 ndel++;
             }
-            mrad = fmax(mrad, cr);
+            mrad = max_bits(mrad, cr);
             RN[i] = cr;
             P3[i] = vpr;
-            if (!isfinite(cr)) bad = 1;
+            bad |= !finite_bits(cr);
         }
         b.delflag[i] = del;
-        mexp = fmax(mexp, dist);
+        mexp = max_bits(mexp, dist);
         if (path) {  // src/kernels.cu:437-451
             t = x0 - cx;
             double d2 = t * t;
             t = y0 - cy;
-            d2 += t * t;
+            d2 = fma(t, t, d2);
             if (DIM == 3) {
                 t = z0 - cz;
-                d2 += t * t;
+                d2 = fma(t, t, d2);
             }
-            PATHN[i] = PATH[i] + sqrt(d2);
+            PATHN[i] = PATH[i] + sqrt_hn(d2);
         }
-        ERR[i] = fmax(e, ERR[i]);
-        merr = fmax(merr, e);
+        const double ed = __longlong_as_double(e);
+        ERR[i] = fmax(ed, ERR[i]);
+        merr = max(merr, e);
         XN[i] = cx;
         YN[i] = cy;
         P0[i] = vpx;
@@ -363,7 +441,7 @@ __global__ void __launch_bounds__(kBlock) k_correct(Bufs b) {
             ZN[i] = cz;
             P2[i] = vpz;
         }
-        if (!isfinite(cx) || !isfinite(cy) || !isfinite(cz)) bad = 1;
+        bad |= !(finite_bits(cx) && finite_bits(cy) && finite_bits(cz));
         if (b.dbg_ov) b.dbg_ov[i] = ov;
         // leave the accumulators zeroed for the next attempt
         double4_32a zero;
@@ -371,9 +449,9 @@ __global__ void __launch_bounds__(kBlock) k_correct(Bufs b) {
         reinterpret_cast<double4_32a *>(acc)[0] = zero;
         if (gas || flow) reinterpret_cast<double4_32a *>(acc)[1] = zero;
     }
-    const double tErr = block_reduce(merr, OpMax(), smem);
-    const double tRad = block_reduce(mrad, OpMax(), smem);
-    const double tExp = block_reduce(mexp, OpMax(), smem);
+    const double tErr = block_reduce(__longlong_as_double(merr), OpMax(), smem);
+    const double tRad = block_reduce(__longlong_as_double(mrad), OpMax(), smem);
+    const double tExp = block_reduce(__longlong_as_double(mexp), OpMax(), smem);
     const double tVol = block_reduce(vol, OpSum(), smem);
     const int tDel = block_reduce_int(ndel, ismem);
     const int tBad = block_reduce_int(bad, ismem);
@@ -394,68 +472,7 @@ __global__ void __launch_bounds__(kBlock) k_correct(Bufs b) {
     const double fDel = fold_partials(b.part + 4 * G, G, false, smem);
     const double fBad = fold_partials(b.part + 5 * G, G, false, smem);
     if (threadIdx.x != 0) return;
-    c->done[DC_CORRECT] = 0;
-    c->max_err = fErr;
-    c->max_rad = fRad;
-    c->max_exp = fExp;
-    c->vol_new = fVol;
-    c->ndel = gas ? (int)fDel : 0;
-    c->attempts += 1;
-    c->attempts_this_step += 1;
-    // step(): accept / reject and the new dt, src/simulator.cu:239-246
-    const double tol = k.tol;
-    const int too_large = fErr > tol;
-    const int increase = fErr < 0.45 * tol && c->dt < 10;
-    if (too_large)
-        c->dt *= 0.37;
-    else if (increase)
-        c->dt *= 1.269;
-    c->too_large = too_large;
-    if (fBad > 0.0 || isnan(fErr)) c->status = CB_ERR_NONFINITE;
-    c->need_delete = 0;
-    c->need_search = 0;
-    if (too_large && c->status == CB_OK) {
-        if (c->attempts_this_step >= k.max_attempts) c->status = CB_ERR_MAX_ATTEMPTS;
-        if (c->dt < 1e-300) c->status = CB_ERR_DT_UNDERFLOW;
-    }
-    if (!too_large && !c->no_accept && c->status == CB_OK) {
-        // integrate(): rotation, src/simulator.cu:258-301
-        int *r = c->drole;
-        for (int a = 0; a < DIM; a++) {
-            swap_role(r, RX + a, RXN + a);
-            const int old = r[RVO0 + a];
-            r[RVO0 + a] = r[RV0 + a];
-            r[RV0 + a] = r[RVP0 + a];
-            r[RVP0 + a] = old;
-        }
-        if (gas) {
-            swap_role(r, RR, RRN);
-            const int old = r[RVO3];
-            r[RVO3] = r[RV3];
-            r[RV3] = r[RVP3];
-            r[RVP3] = old;
-        }
-        if (path) swap_role(r, RPATH, RPATHN);
-        c->steps += 1;
-        c->bubble_steps += n;
-        c->attempts_this_step = 0;
-        // time accumulator, src/simulator.cu:311-314
-        c->tfrac += c->dt;
-        c->tint += (unsigned long long)c->tfrac;
-        c->tfrac = c->tfrac - (double)(unsigned long long)c->tfrac;
-        if (gas) {
-            c->max_bubble_radius = fRad;
-            c->need_delete = c->ndel > 0;
-        }
-        c->need_search = fExp >= 0.5 * k.skin;
-    }
-    if (c->graph_mode) {
-        const int ok = c->status == CB_OK;
-        const int accepted = !too_large;
-        set_cond(c->h_delete, ok && accepted && c->need_delete);
-        set_cond(c->h_search, ok && accepted && c->need_search);
-        set_cond(c->h_loop, ok && (too_large || c->steps < c->steps_target));
-    }
+    finish_attempt<DIM>(c, k, fErr, fRad, fExp, fVol, fDel, fBad);
 }
 
 // --------------------------------------------------------------- bootstrap

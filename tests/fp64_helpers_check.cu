@@ -1,0 +1,31 @@
+// Test harness: evaluates the FP64 helpers of the step kernels (rcp_hn,
+// rsqrt_hn, sqrt_hn, min_image) next to CUDA's IEEE division, rsqrt() and
+// sqrt() on the same inputs. Built by tests/test_gpu_math.py.
+#include "../cubble_gb300/csrc/common.cuh"
+
+__global__ void k_check(const double *in, int n, double *out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double a = in[i];
+        out[8 * i + 0] = cbg::rcp_hn(a);
+        out[8 * i + 1] = 1.0 / a;
+        out[8 * i + 2] = cbg::rsqrt_hn(a);
+        out[8 * i + 3] = rsqrt(a);
+        out[8 * i + 4] = cbg::sqrt_hn(a);
+        out[8 * i + 5] = sqrt(a);
+        out[8 * i + 6] = cbg::min_image(a - 50.0, 40.0, 80.0);
+        const double d = a - 50.0, t = 80.0 - fabs(d);
+        out[8 * i + 7] = t * t < d * d ? t * (d < 0 ? 1.0 : -1.0) : d;
+    }
+}
+
+extern "C" int fp64_check(const double *host_in, int n, double *host_out) {
+    double *din = nullptr, *dout = nullptr;
+    if (cudaMalloc(&din, n * sizeof(double)) != cudaSuccess) return 1;
+    if (cudaMalloc(&dout, 8 * n * sizeof(double)) != cudaSuccess) return 1;
+    cudaMemcpy(din, host_in, n * sizeof(double), cudaMemcpyHostToDevice);
+    k_check<<<256, 256>>>(din, n, dout);
+    cudaError_t e = cudaMemcpy(host_out, dout, 8 * n * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaFree(din);
+    cudaFree(dout);
+    return e == cudaSuccess ? 0 : 2;
+}
