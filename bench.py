@@ -144,6 +144,20 @@ def algorithmic_bytes(dim, np_per_n):
             "step": 176.0 + 8.0 * np_per_n}
 
 
+def profiled_traffic(kernel_name):
+    """DRAM bytes per launch of `kernel_name` from the committed ncu summaries
+    in profiles/ (lines "- `name`: traffic_bytes=N"), or None."""
+    import glob
+    import re
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
+        with open(path) as f:
+            for ln in f:
+                m = re.match(r"- `(.+)`: traffic_bytes=(\d+)", ln.strip())
+                if m and m.group(1) == kernel_name:
+                    return int(m.group(2)), os.path.relpath(path, ROOT)
+    return None
+
+
 def state_bytes(st):
     return int(sum(np.asarray(v).nbytes for v in st.values()))
 
@@ -256,9 +270,17 @@ def run_gb300(args, world, rank, local):
     hbm, src = peaks()
     achieved = ab[names[top]] * n_now / (kms[top] * 1e-3) / 1e9
     step_gbs = ab["step"] * n_now / (sum(kms) * 1e-3) / 1e9
+    gas = int(cfg.use_gas_exchange)
+    flow = int(cfg.use_flow)
+    kname = {"predict": "k_predict<%d>" % dim, "correct": "k_correct<%d>" % dim,
+             "pairs": "k_pairs<%d, %d, %d>" % (dim, gas, flow)}[names[top]]
+    tr = profiled_traffic(kname)
     roof = {"bound": "hbm", "kernel": names[top], "achieved": achieved, "peak": hbm,
             "unit": "GB/s", "frac": achieved / hbm, "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs)",
-            "traffic": None,
+            "traffic": tr[0] if tr else None,
+            "traffic_source": ("%s (ncu dram__bytes_read.sum + dram__bytes_write.sum of %s)"
+                               % (tr[1], kname)) if tr else None,
+            "algorithmic_bytes_per_launch": ab[names[top]] * n_now,
             "kernel_ms": dict(zip(names, kms)),
             "algorithmic_bytes_per_bubble": ab,
             "step_achieved_gbs": step_gbs, "step_frac": step_gbs / hbm}
