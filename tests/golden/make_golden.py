@@ -1,0 +1,488 @@
+"""Generates the golden vectors of tests/golden/ by running the REFERENCE's own
+device code (KJLankinen/cubble src/kernels.cu, compiled unmodified by
+oracle/ref/build_ref.py into oracle/_ref/kernels_ref.cubin) on a GB300.
+
+It restates only the host glue of src/simulator.cu that the kernels need
+(launch shapes, the CUB scans as host prefix sums, the pointer rotations) and
+records, for small seeded foams:
+
+  search   wrapOverPeriodicBoundaries -> cellByPosition -> scan ->
+           indexByCell -> reorganizeByIndex -> neighborSearch
+           (src/simulator.cu:60-163): the pair set keyed by bubble index and
+           the wrapped positions;
+  attempt  initGlobals -> preIntegrate -> pairwiseInteraction ->
+           postIntegrate (src/simulator.cu:192-210) on a given pair list:
+           corrected positions and radii, new velocities, error, pathNew,
+           overlap areas, the global sums, the block maxima, the deletion set;
+  boot     the Euler bootstrap of the AB2 history (src/simulator.cu:744-787);
+  delete   an attempt whose bubbles fall below minRad, the rotation of
+           integrate() and removeBubbles() (swapDataCountPairs,
+           addVolumeFixPairs) with the deletion list in ascending order;
+  energy   potentialEnergy (src/kernels.cu:941-957).
+
+Run on the GPU machine (torch provides the device buffers, ctypes the driver API):
+    python tests/golden/make_golden.py [out_dir]
+The .npz files it writes are committed under tests/golden/.
+"""
+import ctypes as C
+import math
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+CUBIN = os.path.join(ROOT, "oracle", "_ref", "kernels_ref.cubin")
+BLOCK, GRID = 384, 5120  # src/data_definitions.h:28-29
+
+DROWS = ["x", "y", "z", "r", "xp", "yp", "zp", "rp", "dxdt", "dydt", "dzdt", "drdt",
+         "dxdtp", "dydtp", "dzdtp", "drdtp", "dxdto", "dydto", "dzdto", "drdto",
+         "path", "pathNew", "error", "flowVx", "flowVy", "flowVz",
+         "savedX", "savedY", "savedZ", "savedR"]
+IROWS = ["wrapCountX", "wrapCountY", "wrapCountZ", "index", "numNeighbors"]
+
+
+class Bubbles(C.Structure):  # src/data_definitions.h:41-153
+    _fields_ = ([(n, C.c_void_p) for n in DROWS] + [(n, C.c_void_p) for n in IROWS]
+                + [("count", C.c_int32), ("stride", C.c_uint64),
+                   ("numDP", C.c_uint64), ("numIP", C.c_uint64)])
+
+
+class Pairs(C.Structure):  # src/data_definitions.h:157-178
+    _fields_ = [("i", C.c_void_p), ("j", C.c_void_p), ("count", C.c_int32),
+                ("stride", C.c_uint64)]
+
+
+class DVec(C.Structure):
+    _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double)]
+
+
+class IVec(C.Structure):
+    _fields_ = [("x", C.c_int32), ("y", C.c_int32), ("z", C.c_int32)]
+
+
+class Constants(C.Structure):  # src/data_definitions.h:183-225
+    _fields_ = [("lbb", DVec), ("tfr", DVec), ("interval", DVec), ("flowLbb", DVec),
+                ("flowTfr", DVec), ("flowVel", DVec),
+                ("averageSurfaceAreaIn", C.c_double), ("minRad", C.c_double),
+                ("fZeroPerMuZero", C.c_double), ("kParameter", C.c_double),
+                ("kappa", C.c_double), ("wallDragStrength", C.c_double),
+                ("skinRadius", C.c_double), ("bubbleVolumeMultiplier", C.c_double),
+                ("dimensionality", C.c_int32), ("xWall", C.c_bool), ("yWall", C.c_bool),
+                ("zWall", C.c_bool)]
+
+
+class Driver:
+    def __init__(self, cubin):
+        import torch
+        self.torch = torch
+        torch.zeros(1, device="cuda")  # primary context current on this thread
+        self.cu = C.CDLL("libcuda.so.1")
+        self.mod = C.c_void_p()
+        self._ok(self.cu.cuModuleLoad(C.byref(self.mod), cubin.encode()), "cuModuleLoad")
+        cnt = C.c_uint()
+        self._ok(self.cu.cuModuleGetFunctionCount(C.byref(cnt), self.mod), "count")
+        funcs = (C.c_void_p * cnt.value)()
+        self._ok(self.cu.cuModuleEnumerateFunctions(funcs, cnt, self.mod), "enumerate")
+        self.funcs = {}
+        for f in funcs:
+            name = C.c_char_p()
+            self._ok(self.cu.cuFuncGetName(C.byref(name), C.c_void_p(f)), "name")
+            self.funcs[name.value.decode()] = C.c_void_p(f)
+
+    @staticmethod
+    def _ok(rc, what):
+        if rc != 0:
+            raise RuntimeError("%s failed: CUresult %d" % (what, rc))
+
+    def func(self, short):
+        key = "%d%s" % (len(short), short)
+        hits = [n for n in self.funcs if n.startswith("_ZN6cubble" + key)]
+        if len(hits) != 1:
+            raise KeyError(short)
+        return self.funcs[hits[0]]
+
+    def global_ptr(self, short):
+        name = "_ZN6cubble%d%sE" % (len(short), short)
+        ptr, size = C.c_uint64(), C.c_size_t()
+        self._ok(self.cu.cuModuleGetGlobal_v2(C.byref(ptr), C.byref(size), self.mod,
+                                              name.encode()), name)
+        return ptr.value, size.value
+
+    def get_global(self, short, ctype):
+        p, _ = self.global_ptr(short)
+        v = ctype()
+        self.sync()
+        self._ok(self.cu.cuMemcpyDtoH_v2(C.byref(v), C.c_uint64(p), C.sizeof(v)), "DtoH")
+        return v.value
+
+    def set_global(self, short, value):
+        p, _ = self.global_ptr(short)
+        self._ok(self.cu.cuMemcpyHtoD_v2(C.c_uint64(p), C.byref(value), C.sizeof(value)), "HtoD")
+
+    def launch(self, short, args, smem=0):
+        params = (C.c_void_p * len(args))(*[C.cast(C.pointer(a), C.c_void_p) for a in args])
+        self._ok(self.cu.cuLaunchKernel(self.func(short), GRID, 1, 1, BLOCK, 1, 1, smem, None,
+                                        params, None), short)
+
+    def sync(self):
+        self._ok(self.cu.cuCtxSynchronize(), "sync")
+
+
+class Foam:
+    """The reference's device state for one foam (Bubbles rows, pairs,
+    temporaries), in torch device buffers."""
+
+    def __init__(self, drv, cfg, n, pair_stride):
+        t = drv.torch
+        self.drv, self.cfg, self.n = drv, cfg, n
+        self.stride = n + (32 - n % 32) % 32
+        dev = "cuda"
+        self.d = {k: t.zeros(self.stride, dtype=t.float64, device=dev) for k in DROWS}
+        self.i = {k: t.zeros(self.stride, dtype=t.int32, device=dev) for k in IROWS}
+        self.pstride = pair_stride
+        self.pi = t.zeros(pair_stride, dtype=t.int32, device=dev)
+        self.pj = t.zeros(pair_stride, dtype=t.int32, device=dev)
+        self.tmpi = t.zeros(max(self.stride, 1) * 2, dtype=t.int32, device=dev)
+        self.tempD1 = t.zeros(self.stride, dtype=t.float64, device=dev)
+        self.blockMax = t.zeros(3 * GRID, dtype=t.float64, device=dev)
+        self.const = t.zeros(C.sizeof(Constants), dtype=t.uint8, device=dev)
+        self.np = 0
+        k = Constants()
+        dim = cfg.dimensionality
+        k.lbb = DVec(*cfg.lbb)
+        k.tfr = DVec(*cfg.tfr)
+        k.interval = DVec(*[cfg.tfr[a] - cfg.lbb[a] for a in range(3)])
+        k.flowLbb = DVec(*cfg.flow_lbb)
+        k.flowTfr = DVec(*cfg.flow_tfr)
+        k.flowVel = DVec(*cfg.flow_vel)
+        k.averageSurfaceAreaIn = cfg.average_surface_area_in
+        k.minRad = cfg.min_rad
+        k.fZeroPerMuZero = cfg.f0_per_mu0
+        k.kParameter = cfg.k_parameter
+        k.kappa = cfg.kappa
+        k.wallDragStrength = cfg.wall_drag
+        k.skinRadius = cfg.skin_radius
+        k.bubbleVolumeMultiplier = cfg.bubble_volume_multiplier
+        k.dimensionality = dim
+        k.xWall, k.yWall, k.zWall = (bool(w) for w in cfg.wall)
+        host = t.frombuffer(bytearray(bytes(k)), dtype=t.uint8)
+        self.const.copy_(host)
+        drv.set_global("dConstants", C.c_uint64(self.const.data_ptr()))
+        drv.set_global("dNumPairs", C.c_int32(0))
+        drv.launch("initGlobals", [])
+
+    def bubbles(self):
+        b = Bubbles()
+        for k in DROWS:
+            setattr(b, k, self.d[k].data_ptr())
+        for k in IROWS:
+            setattr(b, k, self.i[k].data_ptr())
+        b.count = self.n
+        b.stride = self.stride
+        b.numDP, b.numIP = 30, 5
+        return b
+
+    def pairs(self):
+        p = Pairs()
+        p.i, p.j = self.pi.data_ptr(), self.pj.data_ptr()
+        p.count = self.np
+        p.stride = self.pstride
+        return p
+
+    def put(self, key, arr):
+        t = self.drv.torch
+        src = t.from_numpy(np.ascontiguousarray(arr))
+        (self.d if key in self.d else self.i)[key][:len(arr)].copy_(src)
+
+    def get(self, key, n=None):
+        n = self.n if n is None else n
+        return (self.d if key in self.d else self.i)[key][:n].cpu().numpy().copy()
+
+    def set_pairs(self, i, j):
+        t = self.drv.torch
+        self.pi[:len(i)].copy_(t.from_numpy(np.asarray(i, np.int32)))
+        self.pj[:len(j)].copy_(t.from_numpy(np.asarray(j, np.int32)))
+        self.np = len(i)
+        self.drv.set_global("dNumPairs", C.c_int32(self.np))
+
+    def swap(self, a, b):
+        self.d[a], self.d[b] = self.d[b], self.d[a]
+
+
+def load(f, st):
+    for k_ref, k_st in (("x", "x"), ("y", "y"), ("z", "z"), ("r", "r"),
+                        ("dxdt", "dxdt"), ("dydt", "dydt"), ("dzdt", "dzdt"), ("drdt", "drdt"),
+                        ("dxdto", "dxdto"), ("dydto", "dydto"), ("dzdto", "dzdto"),
+                        ("drdto", "drdto"), ("path", "path"), ("error", "error"),
+                        ("savedX", "saved_x"), ("savedY", "saved_y"), ("savedZ", "saved_z"),
+                        ("savedR", "saved_r")):
+        if k_st in st:
+            f.put(k_ref, st[k_st])
+    for k_ref, k_st in (("index", "index"), ("numNeighbors", "num_neighbors")):
+        if k_st in st:
+            f.put(k_ref, st[k_st].astype(np.int32))
+    f.put("rp", st["r"])  # rp == r before the first step (src/simulator.cu:737-742)
+
+
+# ------------------------------------------------------------------ flows
+def ref_search(drv, cfg, st):
+    """searchNeighbors() (src/simulator.cu:60-163) up to the unsorted pairs."""
+    n = len(st["x"])
+    f = Foam(drv, cfg, n, 64 * n + 64)
+    load(f, st)
+    drv.launch("wrapOverPeriodicBoundaries", [f.bubbles()])
+    iv = np.array([cfg.tfr[a] - cfg.lbb[a] for a in range(3)])
+    max_r = float(np.max(st["r"]))
+    cd = np.floor(iv / (2 * (max_r + cfg.skin_radius))).astype(int)
+    cd[2] = cd[2] if cd[2] > 0 else 1
+    ncell = int(cd[0] * cd[1] * cd[2])
+    t = drv.torch
+    cell_idx = t.zeros(n, dtype=t.int32, device="cuda")
+    sizes = t.zeros(ncell, dtype=t.int32, device="cuda")
+    drv.launch("cellByPosition", [C.c_void_p(cell_idx.data_ptr()), C.c_void_p(sizes.data_ptr()),
+                                  IVec(*cd.tolist()), f.bubbles()])
+    drv.sync()
+    offsets = t.cumsum(sizes, 0, dtype=t.int32)  # CUB InclusiveSum, :90-91
+    bidx = t.zeros(n, dtype=t.int32, device="cuda")
+    off_work = offsets.clone()
+    drv.launch("indexByCell", [C.c_void_p(cell_idx.data_ptr()), C.c_void_p(off_work.data_ptr()),
+                               C.c_void_p(bidx.data_ptr()), C.c_int32(n)])
+    drv.launch("reorganizeByIndex", [f.bubbles(), C.c_void_p(bidx.data_ptr())])
+    drv.sync()
+    # host pointer rotation, src/simulator.cu:99-146
+    for a, b in (("xp", "x"), ("yp", "y"), ("zp", "z"), ("rp", "r"), ("dxdtp", "dxdt"),
+                 ("dydtp", "dydt"), ("dzdtp", "dzdt"), ("drdtp", "drdt")):
+        f.swap(a, b)
+    d = f.d
+    sw = d["error"]
+    d["error"], d["path"], d["drdto"], d["dzdto"], d["dydto"], d["dxdto"], d["flowVx"] = \
+        d["path"], d["drdto"], d["dzdto"], d["dydto"], d["dxdto"], d["flowVx"], sw
+    ii = f.i
+    swi = ii["index"]
+    ii["index"], ii["wrapCountZ"], ii["wrapCountY"], ii["wrapCountX"], ii["numNeighbors"] = \
+        ii["wrapCountZ"], ii["wrapCountY"], ii["wrapCountX"], ii["numNeighbors"], swi
+    drv.set_global("dNumPairs", C.c_int32(0))
+    # offsets after indexByCell hold the cell starts (atomicSub down to them)
+    hist = t.zeros(n, dtype=t.int32, device="cuda")
+    ncs = 14 if cfg.dimensionality == 3 else 5
+    drv.launch("neighborSearch", [C.c_int32(ncell), C.c_int32(ncs), IVec(*cd.tolist()),
+                                  C.c_void_p(off_work.data_ptr()), C.c_void_p(sizes.data_ptr()),
+                                  C.c_void_p(hist.data_ptr()), C.c_void_p(f.pi.data_ptr()),
+                                  C.c_void_p(f.pj.data_ptr()), f.bubbles()])
+    npairs = drv.get_global("dNumPairs", C.c_int32)
+    index = f.get("index")
+    pi = f.pi[:npairs].cpu().numpy()
+    pj = f.pj[:npairs].cpu().numpy()
+    a, b = index[pi], index[pj]
+    pairs = np.stack([np.minimum(a, b), np.maximum(a, b)], 1)
+    pairs = pairs[np.lexsort((pairs[:, 1], pairs[:, 0]))]
+    order = np.argsort(index)
+    wrapped = {k: f.get(k)[order] for k in ("x", "y", "z")}
+    wc = {k: f.get(k)[order] for k in ("wrapCountX", "wrapCountY", "wrapCountZ")}
+    return pairs, wrapped, wc, cd
+
+
+def ref_attempt(drv, cfg, st, pi, pj, ts, gas=True, flow=False, path=True):
+    """step() kernels (src/simulator.cu:197-210) on the given pair list."""
+    n = len(st["x"])
+    f = Foam(drv, cfg, n, max(len(pi), 1))
+    load(f, st)
+    f.set_pairs(pi, pj)
+    return f, attempt_on(drv, cfg, f, ts, gas, flow, path)
+
+
+def attempt_on(drv, cfg, f, ts, gas, flow, path):
+    dim = cfg.dimensionality
+    t = drv.torch
+    tbd = t.zeros(2 * f.stride, dtype=t.int32, device="cuda")
+    f.tbd = tbd
+    drv.launch("initGlobals", [])
+    drv.launch("preIntegrate", [C.c_double(ts), C.c_bool(gas), f.bubbles(),
+                                C.c_void_p(f.tempD1.data_ptr())])
+    smem = (dim + 4 * int(gas) + dim * int(flow)) * BLOCK * 8
+    drv.launch("pairwiseInteraction", [f.bubbles(), f.pairs(), C.c_void_p(f.tempD1.data_ptr()),
+                                       C.c_bool(gas), C.c_bool(flow)], smem)
+    drv.launch("postIntegrate", [C.c_double(ts), C.c_bool(gas), C.c_bool(path), C.c_bool(flow),
+                                 f.bubbles(), C.c_void_p(f.blockMax.data_ptr()),
+                                 C.c_void_p(f.tempD1.data_ptr()), C.c_void_p(tbd.data_ptr())])
+    drv.sync()
+    out = {k: f.get(k) for k in ("xp", "yp", "zp", "rp", "dxdtp", "dydtp", "dzdtp", "drdtp",
+                                 "error", "pathNew")}
+    out["overlap"] = f.tempD1[:f.n].cpu().numpy()
+    for g in ("TotalArea", "TotalAreaPerRadius", "TotalOverlapArea",
+              "TotalOverlapAreaPerRadius", "TotalVolumeNew"):
+        out[g] = np.array(drv.get_global("d" + g, C.c_double))
+    ntbd = drv.get_global("dNumToBeDeleted", C.c_int32)
+    out["to_be_deleted"] = np.sort(tbd[:ntbd].cpu().numpy()) if gas else np.zeros(0, np.int32)
+    bm = f.blockMax.cpu().numpy()
+    nb = min(max(1, math.ceil(f.n / BLOCK)), GRID)
+    out["max_error"] = np.array(bm[:nb].max())
+    out["max_radius"] = np.array(bm[GRID:GRID + nb].max())
+    out["max_expansion"] = np.array(bm[2 * GRID:2 * GRID + nb].max())
+    return out
+
+
+def ref_bootstrap(drv, cfg, st, pi, pj, ts):
+    """init()'s Euler bootstrap (src/simulator.cu:727-787): returns dxdto.."""
+    n = len(st["x"])
+    f = Foam(drv, cfg, n, max(len(pi), 1))
+    load(f, st)
+    f.set_pairs(pi, pj)
+    for k in ("x", "y", "z", "r"):
+        f.d[k[0] + "p" if k != "r" else "rp"].copy_(f.d[k])
+    for k in ("dxdto", "dydto", "dzdto", "drdto", "dxdtp", "dydtp", "dzdtp", "drdtp", "path"):
+        f.d[k].zero_()
+    smem = cfg.dimensionality * BLOCK * 8
+    args = lambda: [f.bubbles(), f.pairs(), C.c_void_p(f.tempD1.data_ptr()),  # noqa: E731
+                    C.c_bool(False), C.c_bool(False)]
+    drv.launch("pairwiseInteraction", args(), smem)
+    drv.launch("euler", [C.c_double(ts), f.bubbles()])
+    for a, b in (("dxdto", "dxdtp"), ("dydto", "dydtp"), ("dzdto", "dzdtp")):
+        f.swap(a, b)
+    drv.launch("pairwiseInteraction", args(), smem)
+    drv.sync()
+    for a, b in (("dxdto", "dxdtp"), ("dydto", "dydtp"), ("dzdto", "dzdtp")):
+        f.swap(a, b)
+    return {k: f.get(k) for k in ("dxdto", "dydto", "dzdto")}
+
+
+def ref_delete(drv, cfg, st, pi, pj, ts):
+    """An accepted attempt with deletions: rotation of integrate()
+    (src/simulator.cu:258-301) then removeBubbles() with the deletion list
+    in ascending order."""
+    n = len(st["x"])
+    f, out = ref_attempt(drv, cfg, st, pi, pj, ts)
+    for a, b in (("x", "xp"), ("y", "yp"), ("z", "zp"), ("r", "rp"), ("path", "pathNew")):
+        f.swap(a, b)
+    for ax in ("x", "y", "z", "r"):
+        o, c, p = "d%sdto" % ax, "d%sdt" % ax, "d%sdtp" % ax
+        f.d[o], f.d[c], f.d[p] = f.d[c], f.d[p], f.d[o]
+    tbd = out["to_be_deleted"].astype(np.int32)
+    D = len(tbd)
+    f.tbd[:D].copy_(drv.torch.from_numpy(tbd))
+    drv.launch("swapDataCountPairs", [f.bubbles(), f.pairs(), C.c_void_p(f.tbd.data_ptr())])
+    drv.launch("addVolumeFixPairs", [f.bubbles(), f.pairs(), C.c_void_p(f.tbd.data_ptr())])
+    drv.sync()
+    nn = n - D
+    npairs = drv.get_global("dNumPairs", C.c_int32)
+    res = {k: f.get(k, nn) for k in ("x", "y", "z", "r", "dxdt", "dydt", "dzdt", "drdt",
+                                      "dxdto", "path", "error", "savedR")}
+    res["index"] = f.get("index", nn)
+    pi2 = f.pi[:npairs].cpu().numpy()
+    pj2 = f.pj[:npairs].cpu().numpy()
+    a, b = res["index"][pi2], res["index"][pj2]
+    pr = np.stack([np.minimum(a, b), np.maximum(a, b)], 1)
+    res["pairs"] = pr[np.lexsort((pr[:, 1], pr[:, 0]))]
+    res["to_be_deleted"] = tbd
+    return res
+
+
+def ref_energy(drv, cfg, st, pi, pj):
+    n = len(st["x"])
+    f = Foam(drv, cfg, n, max(len(pi), 1))
+    load(f, st)
+    f.set_pairs(pi, pj)
+    f.tempD1.zero_()
+    drv.launch("potentialEnergy", [f.bubbles(), f.pairs(), C.c_void_p(f.tempD1.data_ptr())])
+    drv.sync()
+    return f.tempD1[:n].cpu().numpy()
+
+
+# ------------------------------------------------------------------ cases
+def cases():
+    from cubble_gb300 import workloads
+    out = []
+    out.append(("2d", workloads.foam(1200, 2, 0.9, seed=501, min_rad=0.05), {}))
+    out.append(("3d", workloads.foam(1500, 3, 0.8, rstd=0.15, rclip=(0.3, 2.5), seed=502), {}))
+    out.append(("2d_wallx", workloads.foam(1000, 2, 0.85, seed=503, wall=(1, 0, 0),
+                                           wall_drag=0.2), {}))
+    out.append(("3d_wallz", workloads.foam(1200, 3, 0.8, seed=504, wall=(0, 0, 1),
+                                           wall_drag=0.1), {}))
+    return out
+
+
+def oracle_pairs(cfg, st):
+    from oracle.oracle import OracleFoam
+    o = OracleFoam(cfg)
+    o.load_state(st)
+    o.search_neighbors()
+    s = o.get_state()
+    i, j = o.pairs()
+    return s, i, j
+
+
+def main(out_dir):
+    os.makedirs(out_dir, exist_ok=True)
+    drv = Driver(CUBIN)
+    for name, (cfg, st), _ in cases():
+        rng = np.random.default_rng(7)
+        n = len(st["x"])
+        data = {"cfg_" + f: np.array(getattr(cfg, f)) for f, _ in type(cfg)._fields_}
+        # 1. search on the raw (unwrapped) positions, shifted by up to a box length
+        st_s = dict(st)
+        for a, k in enumerate(("x", "y", "z")):
+            if a < cfg.dimensionality and not cfg.wall[a]:
+                L = cfg.tfr[a] - cfg.lbb[a]
+                # only bubbles well inside the box move out by one box length,
+                # so the reference's wrap lands strictly inside [lbb, tfr)
+                inner = (st[k] > cfg.lbb[a] + 0.01 * L) & (st[k] < cfg.tfr[a] - 0.01 * L)
+                sh = rng.integers(-1, 2, n) * L * ((rng.random(n) < 0.05) & inner)
+                st_s[k] = st[k] + sh
+        pairs, wrapped, wc, cd = ref_search(drv, cfg, st_s)
+        for k in ("x", "y", "z", "r"):
+            data["search_in_" + k] = st_s[k]
+        data["search_pairs"] = pairs
+        for k, v in list(wrapped.items()) + list(wc.items()):
+            data["search_out_" + k] = v
+        data["search_ref_cell_dims"] = cd
+        # 2. an attempt from a searched, bootstrapped, moving state
+        s, pi, pj = oracle_pairs(cfg, st)
+        ts = 1e-3
+        st_a = {k: s[k] for k in ("x", "y", "z", "r", "saved_x", "saved_y", "saved_z", "saved_r",
+                                   "index", "num_neighbors")}
+        for k in ("dxdt", "dydt", "dzdt", "dxdto", "dydto", "dzdto"):
+            st_a[k] = rng.normal(0.0, 0.05, n) * (k[1] != "z" or cfg.dimensionality == 3)
+        st_a["drdt"] = rng.normal(0.0, 0.01, n)
+        st_a["drdto"] = rng.normal(0.0, 0.01, n)
+        st_a["path"] = rng.random(n)
+        st_a["error"] = rng.random(n) * 1e-6
+        for k, v in st_a.items():
+            data["attempt_in_" + k] = v
+        data["attempt_pi"], data["attempt_pj"] = pi, pj
+        data["attempt_ts"] = np.array(ts)
+        _, out = ref_attempt(drv, cfg, st_a, pi, pj, ts)
+        for k, v in out.items():
+            data["attempt_out_" + k] = v
+        # 3. bootstrap
+        bo = ref_bootstrap(drv, cfg, st_a, pi, pj, 1e-4)
+        data["boot_ts"] = np.array(1e-4)
+        for k, v in bo.items():
+            data["boot_out_" + k] = v
+        # 4. energy
+        data["energy_out"] = ref_energy(drv, cfg, st_a, pi, pj)
+        # 5. deletion: shrink a few bubbles below minRad
+        st_d = dict(st_a)
+        r = st_d["r"].copy()
+        doomed = rng.choice(n, size=max(3, n // 100), replace=False)
+        r[doomed] = 0.5 * cfg.min_rad
+        st_d["r"] = r
+        st_d["saved_r"] = r
+        st_d["drdt"] = np.zeros(n)
+        st_d["drdto"] = np.zeros(n)
+        st_d["error"] = np.zeros(n)
+        for k, v in st_d.items():
+            data["delete_in_" + k] = v
+        res = ref_delete(drv, cfg, st_d, pi, pj, 1e-5)
+        for k, v in res.items():
+            data["delete_out_" + k] = v
+        path = os.path.join(out_dir, "ref_%s.npz" % name)
+        np.savez_compressed(path, **data)
+        print("wrote", path, "pairs", len(pairs), "deleted", len(res["to_be_deleted"]))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "gpurun_out", "golden"))

@@ -1,0 +1,151 @@
+"""CPU: the oracle against golden vectors recorded from the REFERENCE's own
+kernels (src/kernels.cu compiled unmodified and run on a GB300 by
+tests/golden/make_golden.py): neighbour search, one step attempt, the Euler
+bootstrap, the potential energy and a deletion with the volume fix.
+
+Bars: pair sets, deletion sets, compaction order and wrapped positions
+bit-exact; floating-point rows within 1e-12 of the row's largest magnitude
+(the reference sums per-bubble contributions with atomics, so only the order
+of FP64 additions differs)."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from cubble_gb300 import _abi
+from cubble_gb300.foam import make_config
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+FILES = sorted(glob.glob(os.path.join(HERE, "golden", "ref_*.npz")))
+
+
+def load(path):
+    return dict(np.load(path))
+
+
+def config(d, **over):
+    kw = {}
+    for f, _ in _abi.Config._fields_:
+        v = d["cfg_" + f]
+        kw[f] = v.tolist() if v.ndim else v.item()
+    kw.update(over)
+    return make_config(**kw)
+
+
+def state(d, prefix):
+    out = {}
+    for k in ("x", "y", "z", "r", "dxdt", "dydt", "dzdt", "drdt", "dxdto", "dydto", "dzdto",
+              "drdto", "path", "error", "saved_x", "saved_y", "saved_z", "saved_r"):
+        if prefix + k in d:
+            out[k] = d[prefix + k]
+    for k in ("index", "num_neighbors"):
+        if prefix + k in d:
+            out[k] = d[prefix + k].astype(np.int32)
+    if "index" not in out:
+        out["index"] = np.arange(len(out["x"]), dtype=np.int32)
+    return out
+
+
+def rel(a, b):
+    scale = max(float(np.max(np.abs(b))), 1e-300)
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b)))) / scale
+
+
+ids = [os.path.basename(f)[4:-4] for f in FILES]
+
+
+def test_golden_files_present():
+    assert len(FILES) >= 4
+
+
+@pytest.mark.parametrize("path", FILES, ids=ids)
+def test_search_matches_reference(oracle_mod, path):
+    d = load(path)
+    cfg = config(d)
+    f = oracle_mod.OracleFoam(cfg)
+    st = state(d, "search_in_")
+    f.load_state(st)
+    f.search_neighbors()
+    s = f.get_state()
+    i, j = f.pairs()
+    a, b = s["index"][i], s["index"][j]
+    got = np.stack([np.minimum(a, b), np.maximum(a, b)], 1)
+    got = got[np.lexsort((got[:, 1], got[:, 0]))]
+    assert np.array_equal(got, d["search_pairs"])
+    order = np.argsort(s["index"])
+    for k, kw in (("x", "wrapCountX"), ("y", "wrapCountY"), ("z", "wrapCountZ")):
+        assert np.array_equal(s[k][order], d["search_out_" + k]), k
+        assert np.array_equal(s["wrap_count_" + k][order], d["search_out_" + kw]), kw
+
+
+@pytest.mark.parametrize("path", FILES, ids=ids)
+def test_attempt_matches_reference(oracle_mod, path):
+    d = load(path)
+    cfg = config(d)
+    f = oracle_mod.OracleFoam(cfg)
+    f.load_state(state(d, "attempt_in_"))
+    f.set_pairs(d["attempt_pi"], d["attempt_pj"])
+    f.set_time(float(d["attempt_ts"]))
+    out = f.attempt()
+    for mine, ref in (("xp", "xp"), ("yp", "yp"), ("zp", "zp"), ("rp", "rp"),
+                      ("dxdtp", "dxdtp"), ("dydtp", "dydtp"), ("dzdtp", "dzdtp"),
+                      ("drdtp", "drdtp"), ("error", "error"), ("path_new", "pathNew"),
+                      ("overlap", "overlap")):
+        if cfg.dimensionality == 2 and mine in ("zp", "dzdtp"):
+            continue
+        assert rel(out[mine], d["attempt_out_" + ref]) <= 1e-12, mine
+    for mine, ref in (("total_area", "TotalArea"), ("total_area_per_radius", "TotalAreaPerRadius"),
+                      ("total_overlap_area", "TotalOverlapArea"),
+                      ("total_overlap_area_per_radius", "TotalOverlapAreaPerRadius"),
+                      ("total_volume_new", "TotalVolumeNew"), ("max_error", "max_error"),
+                      ("max_radius", "max_radius"), ("max_expansion", "max_expansion")):
+        assert out[mine] == pytest.approx(float(d["attempt_out_" + ref]), rel=1e-12), mine
+    assert np.array_equal(np.flatnonzero(out["delete_flags"]), d["attempt_out_to_be_deleted"])
+
+
+@pytest.mark.parametrize("path", FILES, ids=ids)
+def test_bootstrap_matches_reference(oracle_mod, path):
+    d = load(path)
+    cfg = config(d, time_step=float(d["boot_ts"]))
+    f = oracle_mod.OracleFoam(cfg)
+    f.load_state(state(d, "attempt_in_"))
+    f.set_pairs(d["attempt_pi"], d["attempt_pj"])
+    f.bootstrap()
+    s = f.get_state()
+    for k in ("dxdto", "dydto") + (("dzdto",) if cfg.dimensionality == 3 else ()):
+        assert rel(s[k], d["boot_out_" + k]) <= 1e-12, k
+
+
+@pytest.mark.parametrize("path", FILES, ids=ids)
+def test_energy_matches_reference(oracle_mod, path):
+    d = load(path)
+    f = oracle_mod.OracleFoam(config(d))
+    f.load_state(state(d, "attempt_in_"))
+    f.set_pairs(d["attempt_pi"], d["attempt_pj"])
+    assert rel(f.bubble_energies(), d["energy_out"]) <= 1e-12
+
+
+@pytest.mark.parametrize("path", FILES, ids=ids)
+def test_deletion_matches_reference(oracle_mod, path):
+    d = load(path)
+    # one accepted step, no search afterwards: the same work the harness did
+    cfg = config(d, error_tolerance=1.0, skin_radius=1e9, time_step=1e-5)
+    f = oracle_mod.OracleFoam(cfg)
+    f.load_state(state(d, "delete_in_"))
+    f.set_pairs(d["attempt_pi"], d["attempt_pj"])
+    rep = f.integrate(1)
+    assert rep["deleted"] == len(d["delete_out_to_be_deleted"])
+    s = f.get_state()
+    assert np.array_equal(s["index"], d["delete_out_index"])
+    for k, ref in (("x", "x"), ("y", "y"), ("z", "z"), ("r", "r"), ("dxdt", "dxdt"),
+                   ("drdt", "drdt"), ("dxdto", "dxdto"), ("path", "path"),
+                   ("error", "error"), ("saved_r", "savedR")):
+        if cfg.dimensionality == 2 and k == "z":
+            continue
+        assert rel(s[k], d["delete_out_" + ref]) <= 1e-12, k
+    i, j = f.pairs()
+    a, b = s["index"][i], s["index"][j]
+    got = np.stack([np.minimum(a, b), np.maximum(a, b)], 1)
+    got = got[np.lexsort((got[:, 1], got[:, 0]))]
+    assert np.array_equal(got, d["delete_out_pairs"])
