@@ -144,6 +144,22 @@ void fill_const(cb_context *c) {
         k.half_iv32[a] = (float)(0.5 * k.iv[a]);
         k.iv32[a] = (float)k.iv[a];
     }
+    k.mixed = f.precision == CB_PRECISION_MIXED ? 1 : 0;
+    for (int a = 0; a < 3; a++) {
+        const double iv = k.iv[a];
+        if (iv <= 0.0) {
+            k.fx_scale[a] = k.fx_off[a] = 0.0;
+            k.fx_inv[a] = 0.f;
+        } else if (!k.wall[a]) {  // q = (x - lbb) 2^32 / L, wraps mod 2^32
+            k.fx_scale[a] = 4294967296.0 / iv;
+            k.fx_off[a] = -k.lbb[a] * k.fx_scale[a];
+            k.fx_inv[a] = (float)(iv / 4294967296.0);
+        } else {  // q = (x - lbb + L/4) 2^30 / (1.5 L), no wrap
+            k.fx_scale[a] = 1073741824.0 / (1.5 * iv);
+            k.fx_off[a] = -(k.lbb[a] - 0.25 * iv) * k.fx_scale[a];
+            k.fx_inv[a] = (float)(1.5 * iv / 1073741824.0);
+        }
+    }
     // FP32 coordinates carry |x| 2^-24 rounding; 1e-5 (maxabs + interval) is
     // more than 20x the worst error of the prefiltered distance.
     k.pre_margin = (float)(1e-5 * (maxabs + maxiv) + 1e-4);
@@ -156,11 +172,22 @@ int sync_status(cb_context *c) {
     return CB_OK;
 }
 
-int run_attempt(cb_context *c) {
+// The three kernels of one step() attempt, in the context's precision.
+void launch_attempt_kernels(const cb_context *c, const Launch &l, const Bufs &b, int which = 7) {
     const int dim = c->hk.dim;
-    launch_predict(c->launch, c->bufs, dim);
-    launch_pairs(c->launch, c->bufs, dim, c->mode());
-    launch_correct(c->launch, c->bufs, dim);
+    if (c->hk.mixed) {
+        if (which & 1) launch_predict_mx(l, b, dim);
+        if (which & 2) launch_pairs_mx(l, b, dim, c->mode());
+        if (which & 4) launch_correct_mx(l, b, dim);
+    } else {
+        if (which & 1) launch_predict(l, b, dim);
+        if (which & 2) launch_pairs(l, b, dim, c->mode());
+        if (which & 4) launch_correct(l, b, dim);
+    }
+}
+
+int run_attempt(cb_context *c) {
+    launch_attempt_kernels(c, c->launch, c->bufs);
     return c->check_launch();
 }
 
@@ -248,9 +275,7 @@ int build_graph(cb_context *c) {
     CB_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0,
                                           cudaStreamCaptureModeThreadLocal));
     const int dim = c->hk.dim;
-    launch_predict(l, c->bufs, dim);
-    launch_pairs(l, c->bufs, dim, c->mode());
-    launch_correct(l, c->bufs, dim);
+    launch_attempt_kernels(c, l, c->bufs);
     cudaGraph_t delbody, searchbody;
     int rc = capture_conditional(s, cudaGraphCondTypeIf, &hdel, 0, &delbody);
     if (!rc) rc = capture_conditional(s, cudaGraphCondTypeIf, &hsearch, 0, &searchbody);
@@ -471,12 +496,19 @@ int cb_load_state(cb_context *c, const cb_state_view *s) {
     drows[RS1] = s->saved_y ? s->saved_y : s->y;
     drows[RS2] = s->saved_z ? s->saved_z : s->z;
     drows[RS3] = s->saved_r ? s->saved_r : s->r;
+    std::vector<std::vector<float>> fl;
     for (int r = 0; r < ND_ROLES; r++) {
         double *dst = c->dslot[h.drole[r]];
-        if (drows[r])
+        const bool rate = r >= RV0 && r <= RVP3;
+        if (drows[r] && c->hk.mixed && rate) {  // FP32 rate rows
+            fl.emplace_back(drows[r], drows[r] + n);
+            CB_CUDA(cudaMemcpyAsync(dst, fl.back().data(), n * 4, cudaMemcpyHostToDevice,
+                                    c->stream));
+        } else if (drows[r]) {
             CB_CUDA(cudaMemcpyAsync(dst, drows[r], n * 8, cudaMemcpyHostToDevice, c->stream));
-        else
+        } else {
             CB_CUDA(cudaMemsetAsync(dst, 0, (size_t)c->hk.cap * 8, c->stream));
+        }
     }
     const int32_t *irows[NI_ROLES] = {};
     irows[IWX] = s->wrap_count_x;
@@ -538,10 +570,18 @@ int cb_get_state(cb_context *c, cb_state_view *s) {
     drows[RS1] = s->saved_y;
     drows[RS2] = s->saved_z;
     drows[RS3] = s->saved_r;
-    for (int r = 0; r < ND_ROLES; r++)
-        if (drows[r] && n)
-            CB_CUDA(cudaMemcpyAsync(drows[r], c->dslot[h.drole[r]], n * 8, cudaMemcpyDeviceToHost,
-                                    c->stream));
+    std::vector<std::pair<double *, std::vector<float>>> fl;
+    for (int r = 0; r < ND_ROLES; r++) {
+        if (!drows[r] || !n) continue;
+        if (c->hk.mixed && r >= RV0 && r <= RVP3) {  // FP32 rate rows
+            fl.emplace_back(drows[r], std::vector<float>(n));
+            CB_CUDA(cudaMemcpyAsync(fl.back().second.data(), c->dslot[h.drole[r]], n * 4,
+                                    cudaMemcpyDeviceToHost, c->stream));
+            continue;
+        }
+        CB_CUDA(cudaMemcpyAsync(drows[r], c->dslot[h.drole[r]], n * 8, cudaMemcpyDeviceToHost,
+                                c->stream));
+    }
     int32_t *irows[NI_ROLES] = {};
     irows[IWX] = s->wrap_count_x;
     irows[IWY] = s->wrap_count_y;
@@ -553,6 +593,8 @@ int cb_get_state(cb_context *c, cb_state_view *s) {
             CB_CUDA(cudaMemcpyAsync(irows[r], c->islot[h.irole[r]], n * 4, cudaMemcpyDeviceToHost,
                                     c->stream));
     CB_CUDA(cudaStreamSynchronize(c->stream));
+    for (auto &f : fl)
+        for (size_t i = 0; i < n; i++) f.first[i] = f.second[i];
     return CB_OK;
 }
 
@@ -595,11 +637,19 @@ int cb_bootstrap(cb_context *c) {
     CB_ENTER(c);
     if (!c->loaded) return fail(CB_ERR_STATE, "state not loaded");
     const int dim = c->hk.dim;
-    launch_boot(c->launch, c->bufs, dim, 0);
-    launch_pairs(c->launch, c->bufs, dim, 0);
-    launch_boot(c->launch, c->bufs, dim, 1);
-    launch_pairs(c->launch, c->bufs, dim, 0);
-    launch_boot(c->launch, c->bufs, dim, 2);
+    if (c->hk.mixed) {
+        launch_boot_mx(c->launch, c->bufs, dim, 0);
+        launch_pairs_mx(c->launch, c->bufs, dim, 0);
+        launch_boot_mx(c->launch, c->bufs, dim, 1);
+        launch_pairs_mx(c->launch, c->bufs, dim, 0);
+        launch_boot_mx(c->launch, c->bufs, dim, 2);
+    } else {
+        launch_boot(c->launch, c->bufs, dim, 0);
+        launch_pairs(c->launch, c->bufs, dim, 0);
+        launch_boot(c->launch, c->bufs, dim, 1);
+        launch_pairs(c->launch, c->bufs, dim, 0);
+        launch_boot(c->launch, c->bufs, dim, 2);
+    }
     int rc = c->check_launch();
     if (rc) return rc;
     return sync_status(c);
@@ -669,9 +719,7 @@ int cb_attempt(cb_context *c, cb_attempt_view *o) {
     Bufs b = c->bufs;
     b.dbg_ov = c->bufs.energy;  // scratch row for the overlap copy
     const int dim = c->hk.dim;
-    launch_predict(c->launch, b, dim);
-    launch_pairs(c->launch, b, dim, c->mode());
-    launch_correct(c->launch, b, dim);
+    launch_attempt_kernels(c, c->launch, b);
     if ((rc = c->check_launch())) return rc;
     if ((rc = c->pull())) return rc;
     Ctrl &h = *c->hctrl;
@@ -682,9 +730,17 @@ int cb_attempt(cb_context *c, cb_attempt_view *o) {
                           o->error, o->path_new, o->overlap};
         const int roles[] = {RXN, RYN, dim == 3 ? RZN : RZ, gas ? RRN : RR, RVP0, RVP1,
                              RVP2, RVP3, RERR, RPATHN, -1};
+        std::vector<float> tmp;
         for (int q = 0; q < 11; q++) {
             if (!rows[q] || !n) continue;
             const double *src = roles[q] >= 0 ? c->dslot[h.drole[roles[q]]] : c->bufs.energy;
+            if (c->hk.mixed && q >= 4 && q < 8) {  // FP32 rate rows
+                tmp.resize(n);
+                CB_CUDA(cudaMemcpyAsync(tmp.data(), src, n * 4, cudaMemcpyDeviceToHost, c->stream));
+                CB_CUDA(cudaStreamSynchronize(c->stream));
+                for (size_t i = 0; i < n; i++) rows[q][i] = tmp[i];
+                continue;
+            }
             CB_CUDA(cudaMemcpyAsync(rows[q], src, n * 8, cudaMemcpyDeviceToHost, c->stream));
         }
         if (o->delete_flags && n)
@@ -812,11 +868,11 @@ int cb_profile_kernels(cb_context *c, int32_t reps, double ms[3]) {
     const int dim = c->hk.dim;
     for (int r = 0; r < reps; r++) {
         CB_CUDA(cudaEventRecord(ev[0], c->stream));
-        launch_predict(c->launch, c->bufs, dim);
+        launch_attempt_kernels(c, c->launch, c->bufs, 1);
         CB_CUDA(cudaEventRecord(ev[1], c->stream));
-        launch_pairs(c->launch, c->bufs, dim, c->mode());
+        launch_attempt_kernels(c, c->launch, c->bufs, 2);
         CB_CUDA(cudaEventRecord(ev[2], c->stream));
-        launch_correct(c->launch, c->bufs, dim);
+        launch_attempt_kernels(c, c->launch, c->bufs, 4);
         CB_CUDA(cudaEventRecord(ev[3], c->stream));
         CB_CUDA(cudaEventSynchronize(ev[3]));
         for (int q = 0; q < 3; q++) {

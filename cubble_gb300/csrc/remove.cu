@@ -14,12 +14,6 @@
 namespace cbg {
 namespace {
 
-__device__ __forceinline__ void swap_role(int *r, int a, int b) {
-    const int t = r[a];
-    r[a] = r[b];
-    r[b] = t;
-}
-
 // holes[k] = k-th deleted index below nNew; keep flags of the pairs.
 __global__ void __launch_bounds__(kBlock) k_remove_a(Bufs b) {
     const Ctrl *c = b.ctrl;
@@ -53,7 +47,10 @@ __global__ void __launch_bounds__(kBlock) k_remove_b(Bufs b) {
             const int role = kRoles[q];
             if (DIM == 2 && (role == RZ || role == RV2 || role == RVO2 || role == RS2)) continue;
             double *row = drow(b, c, role);
-            row[dst] = row[i];
+            if (b.k->mixed && role >= RV0 && role <= RVO3)  // FP32 rate rows
+                reinterpret_cast<float *>(row)[dst] = reinterpret_cast<float *>(row)[i];
+            else
+                row[dst] = row[i];
         }
 #pragma unroll
         for (int q = 0; q < (int)(sizeof(kIRoles) / sizeof(int)); q++) {

@@ -22,12 +22,6 @@
 namespace cbg {
 namespace {
 
-__device__ __forceinline__ void swap_role(int *r, int a, int b) {
-    const int t = r[a];
-    r[a] = r[b];
-    r[b] = t;
-}
-
 // Cell grid: cellDim_a = max(1, floor(interval_a / (2 maxR + skin))) on the
 // used axes; while the product exceeds the cell capacity the largest
 // dimension (lowest axis on ties) shrinks by one.
@@ -148,6 +142,20 @@ __global__ void __launch_bounds__(kBlock) k_cell_order(Bufs b) {
     }
 }
 
+// Gathers a rate row (FP64, or FP32 in the mixed form) into another slot.
+__device__ __forceinline__ void gather_rate(const Bufs &b, const Ctrl *c, int from_role,
+                                            int to_role, const int *src, int n) {
+    const bool f32 = b.k->mixed;
+    const double *from = drow(b, c, from_role);
+    double *to = drow(b, c, to_role);
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        if (f32)
+            reinterpret_cast<float *>(to)[q] = reinterpret_cast<const float *>(from)[src[q]];
+        else
+            to[q] = from[src[q]];
+    }
+}
+
 // Gather pass A: positions (+ saved), velocities, path, error, wrap counts
 // and indices into their spare slots, then swap the roles.
 template <int DIM>
@@ -171,10 +179,7 @@ __global__ void __launch_bounds__(kBlock) k_permute_a(Bufs b) {
     }
     for (int a = 0; a < 4; a++) {
         if (DIM == 2 && a == 2) continue;
-        const double *from = drow(b, c, RV0 + a);
-        double *to = drow(b, c, RVP0 + a);
-        for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
-            to[q] = from[src[q]];
+        gather_rate(b, c, RV0 + a, RVP0 + a, src, n);
     }
     {
         const double *f1 = drow(b, c, RPATH), *f2 = drow(b, c, RERR);
@@ -226,10 +231,7 @@ __global__ void __launch_bounds__(kBlock) k_permute_b(Bufs b) {
     const int *src = b.permSorted;
     for (int a = 0; a < 4; a++) {
         if (DIM == 2 && a == 2) continue;
-        const double *from = drow(b, c, RVO0 + a);
-        double *to = drow(b, c, RVP0 + a);
-        for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
-            to[q] = from[src[q]];
+        gather_rate(b, c, RVO0 + a, RVP0 + a, src, n);
     }
     if (last_block(&c->done[DC_PERMUTE]) && threadIdx.x == 0) {
         for (int a = 0; a < 4; a++) {

@@ -19,88 +19,8 @@
 namespace cbg {
 namespace {
 
-__device__ __forceinline__ void swap_role(int *r, int a, int b) {
-    const int t = r[a];
-    r[a] = r[b];
-    r[b] = t;
-}
-
-__device__ __forceinline__ void set_cond(unsigned long long h, unsigned int v) {
-    cudaGraphSetConditional((cudaGraphConditionalHandle)h, v);
-}
-
 __device__ __forceinline__ double4_32a ld4(const double *p, int i) {
     return reinterpret_cast<const double4_32a *>(p)[i];
-}
-
-// step(): accept / reject and the new dt (src/simulator.cu:239-246); on
-// accept, integrate()'s rotation and clock (src/simulator.cu:258-314) and the
-// delete / search decisions (:316-334). Run by one thread of the last block.
-template <int DIM>
-__device__ void finish_attempt(Ctrl *c, const DevConst &k, double fErr, double fRad,
-                               double fExp, double fVol, double fDel, double fBad) {
-    const int gas = c->use_gas, path = c->inc_path;
-    const int n = c->n;
-    c->done[DC_CORRECT] = 0;
-    c->max_err = fErr;
-    c->max_rad = fRad;
-    c->max_exp = fExp;
-    c->vol_new = fVol;
-    c->ndel = gas ? (int)fDel : 0;
-    c->attempts += 1;
-    c->attempts_this_step += 1;
-    const double tol = k.tol;
-    const int too_large = fErr > tol;
-    const int increase = fErr < 0.45 * tol && c->dt < 10;
-    if (too_large)
-        c->dt *= 0.37;
-    else if (increase)
-        c->dt *= 1.269;
-    c->too_large = too_large;
-    if (fBad > 0.0 || isnan(fErr)) c->status = CB_ERR_NONFINITE;
-    c->need_delete = 0;
-    c->need_search = 0;
-    if (too_large && c->status == CB_OK) {
-        if (c->attempts_this_step >= k.max_attempts) c->status = CB_ERR_MAX_ATTEMPTS;
-        if (c->dt < 1e-300) c->status = CB_ERR_DT_UNDERFLOW;
-    }
-    if (!too_large && !c->no_accept && c->status == CB_OK) {
-        int *r = c->drole;
-        for (int a = 0; a < DIM; a++) {
-            swap_role(r, RX + a, RXN + a);
-            const int old = r[RVO0 + a];
-            r[RVO0 + a] = r[RV0 + a];
-            r[RV0 + a] = r[RVP0 + a];
-            r[RVP0 + a] = old;
-        }
-        if (gas) {
-            swap_role(r, RR, RRN);
-            const int old = r[RVO3];
-            r[RVO3] = r[RV3];
-            r[RV3] = r[RVP3];
-            r[RVP3] = old;
-        }
-        if (path) swap_role(r, RPATH, RPATHN);
-        c->steps += 1;
-        c->bubble_steps += n;
-        c->attempts_this_step = 0;
-        // time accumulator, src/simulator.cu:311-314 (adds the updated dt)
-        c->tfrac += c->dt;
-        c->tint += (unsigned long long)c->tfrac;
-        c->tfrac = c->tfrac - (double)(unsigned long long)c->tfrac;
-        if (gas) {
-            c->max_bubble_radius = fRad;
-            c->need_delete = c->ndel > 0;
-        }
-        c->need_search = fExp >= 0.5 * k.skin;
-    }
-    if (c->graph_mode) {
-        const int ok = c->status == CB_OK;
-        const int accepted = !too_large;
-        set_cond(c->h_delete, ok && accepted && c->need_delete);
-        set_cond(c->h_search, ok && accepted && c->need_search);
-        set_cond(c->h_loop, ok && (too_large || c->steps < c->steps_target));
-    }
 }
 
 // ---------------------------------------------------------------- predict
