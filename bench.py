@@ -135,8 +135,25 @@ def allreduce(x, op, world):
     return float(t.item())
 
 
-def algorithmic_bytes(dim, np_per_n):
-    """Algorithmic HBM bytes per bubble of each attempt kernel (FP64 form)."""
+def algorithmic_bytes(dim, np_per_n, mixed=False):
+    """Algorithmic HBM bytes per bubble of each attempt kernel.
+
+    FP64 form, 3D: predict reads x,y,z,r, v x4, v_old x4 (96) and writes the
+    packed prediction + 1/r (40); pairs reads the pair indices (8 P/N), the
+    prediction once (40) and writes the accumulators once (40); correct reads
+    accumulators (40), prediction (32), x (32), v (32), saved (32), path (8),
+    error (8) and writes x' (32), v' (32), path' (8), error (8), clears the
+    accumulators (40). The whole step's compulsory traffic is 224 + 8 P/N.
+    Mixed form (FP32 rates, 32-byte fixed-point prediction, 20-byte FP32
+    accumulators), 3D: predict 64 + 32, pairs 8 P/N + 32 + 20, correct
+    132 + 88; step 176 + 8 P/N (q FP64 r/w 64, f FP32 r/w 32, f_old 16,
+    saved 32, path 16, error 16)."""
+    if mixed:
+        if dim == 3:
+            return {"predict": 96.0, "pairs": 52.0 + 8.0 * np_per_n, "correct": 220.0,
+                    "step": 176.0 + 8.0 * np_per_n}
+        return {"predict": 80.0, "pairs": 48.0 + 8.0 * np_per_n, "correct": 176.0,
+                "step": 136.0 + 8.0 * np_per_n}
     if dim == 3:
         return {"predict": 136.0, "pairs": 80.0 + 8.0 * np_per_n, "correct": 304.0,
                 "step": 224.0 + 8.0 * np_per_n}
@@ -230,13 +247,12 @@ def run_reference(args, world, rank):
     print(json.dumps(line))
 
 
-def run_gb300(args, world, rank, local):
+def measure_form(args, world, rank, precision, clocks_on=True):
+    """Times K accepted steps of one form; returns its numbers."""
     import torch
     import cubble_gb300 as cb
     from cubble_gb300 import workloads
-    torch.cuda.set_device(local)
-    cb.build()
-    cfg, st, desc = workload(args.workload, args.seed + rank, precision=args.precision,
+    cfg, st, desc = workload(args.workload, args.seed + rank, precision=precision,
                              use_graph=args.graph)
     dim = cfg.dimensionality
     sim = cb.GpuFoam(cfg)
@@ -245,38 +261,36 @@ def run_gb300(args, world, rank, local):
     sim.integrate(args.warmup)
     r0 = sim.report()
     l0 = sim.launch_count()
-    clocks = Clocks(local)
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
     barrier(world)
     torch.cuda.synchronize()
-    clocks.start()
+    if clocks_on:
+        clocks.start()
     r1, dev_ms = sim.integrate_timed(args.steps)
     torch.cuda.synchronize()
     barrier(world)
-    clk = clocks.stop()
+    clk = clocks.stop() if clocks_on else None
     launches = sim.launch_count() - l0
     bs = r1["bubble_steps"] - r0["bubble_steps"]
     el = allreduce(dev_ms / 1e3, _op("max"), world)
     bs_all = allreduce(bs, _op("sum"), world)
-    value = bs_all / el
-    attempts = r1["attempts"] - r0["attempts"]
-    searches = r1["searches"] - r0["searches"]
     np_per_n = r1["num_pairs"] / max(r1["count"], 1)
-    # per-kernel device times (CUDA events on the library's stream)
     kms = sim.profile_kernels(reps=5)
     names = ["predict", "pairs", "correct"]
     top = int(np.argmax(kms))
-    ab = algorithmic_bytes(dim, np_per_n)
+    ab = algorithmic_bytes(dim, np_per_n, mixed=bool(precision))
     n_now = r1["count"]
     hbm, src = peaks()
     achieved = ab[names[top]] * n_now / (kms[top] * 1e-3) / 1e9
     step_gbs = ab["step"] * n_now / (sum(kms) * 1e-3) / 1e9
-    gas = int(cfg.use_gas_exchange)
-    flow = int(cfg.use_flow)
-    kname = {"predict": "k_predict<%d>" % dim, "correct": "k_correct<%d>" % dim,
-             "pairs": "k_pairs<%d, %d, %d>" % (dim, gas, flow)}[names[top]]
+    gas, flow = int(cfg.use_gas_exchange), int(cfg.use_flow)
+    sfx = "_mx" if precision else ""
+    kname = {"predict": "k_predict%s<%d>" % (sfx, dim), "correct": "k_correct%s<%d>" % (sfx, dim),
+             "pairs": "k_pairs%s<%d, %d, %d>" % (sfx, dim, gas, flow)}[names[top]]
     tr = profiled_traffic(kname)
-    roof = {"bound": "hbm", "kernel": names[top], "achieved": achieved, "peak": hbm,
-            "unit": "GB/s", "frac": achieved / hbm, "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs)",
+    roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": hbm,
+            "unit": "GB/s", "frac": achieved / hbm,
+            "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs)",
             "traffic": tr[0] if tr else None,
             "traffic_source": ("%s (ncu dram__bytes_read.sum + dram__bytes_write.sum of %s)"
                                % (tr[1], kname)) if tr else None,
@@ -285,6 +299,78 @@ def run_gb300(args, world, rank, local):
             "algorithmic_bytes_per_bubble": ab,
             "step_achieved_gbs": step_gbs, "step_frac": step_gbs / hbm}
     sim.close()
+    return {"value": bs_all / el, "el": el, "cfg": cfg, "st": st, "desc": desc, "r0": r0,
+            "r1": r1, "roofline": roof, "launches": launches, "clocks": clk,
+            "np_per_n": np_per_n}
+
+
+def mixed_errors(args, steps=50):
+    """Per-quantity error of the mixed form against the FP64 form (which
+    matches the FP64 oracle within 1e-12 per step) from the same prepared
+    state: one attempt, then `steps` accepted steps."""
+    import cubble_gb300 as cb
+    from cubble_gb300 import workloads
+    cfg64, st, _ = workload(args.workload, args.seed, precision=0, use_graph=1)
+    cfgmx, _, _ = workload(args.workload, args.seed, precision=1, use_graph=1)
+    a = cb.GpuFoam(cfg64)
+    a.load_state(st)
+    workloads.prepare(a)
+    a.integrate(args.warmup)
+    s0 = a.get_state()
+    i, j = a.pairs()
+    b = cb.GpuFoam(cfgmx)
+    b.load_state(s0)
+    b.set_pairs(i, j)
+    dt = a.report()["time_step"]
+    b.set_time(dt)
+
+    def rel(x, y):
+        return float(np.max(np.abs(x - y)) / max(np.max(np.abs(y)), 1e-300))
+    aa, ab_ = a.attempt(), b.attempt()
+    out = {"attempt": {}}
+    for k, base in (("xp", "x"), ("yp", "y"), ("zp", "z"), ("rp", "r")):
+        out["attempt"]["d" + base] = rel(ab_[k] - s0[base], aa[k] - s0[base])
+    for k in ("dxdtp", "dydtp", "dzdtp", "drdtp", "overlap"):
+        out["attempt"][k] = rel(ab_[k], aa[k])
+    for k in ("total_area", "total_overlap_area", "total_overlap_area_per_radius"):
+        out["attempt"][k] = abs(ab_[k] / aa[k] - 1.0)
+    out["attempt"]["max_error"] = abs(ab_["max_error"] / aa["max_error"] - 1.0)
+    a.set_time(dt)
+    b.set_time(dt)
+    v0 = a.total_volume()
+    ra0, rb0 = a.report(), b.report()
+    ra, rb = a.integrate(steps), b.integrate(steps)
+    sa, sb = a.get_state(), b.get_state()
+    oa_, ob_ = np.argsort(sa["index"]), np.argsort(sb["index"])
+    o0 = np.argsort(s0["index"])
+    traj = {"steps": steps,
+            "same_attempts_searches_deletions": all(
+                ra[k] - ra0[k] == rb[k] - rb0[k] for k in ("attempts", "searches", "deleted"))}
+    for k in ("x", "y", "z"):
+        traj["d" + k] = rel(sb[k][ob_] - s0[k][o0], sa[k][oa_] - s0[k][o0])
+    traj["r"] = rel(sb["r"][ob_], sa["r"][oa_])
+    traj["volume_drift"] = abs(b.total_volume() / a.total_volume() - 1.0)
+    traj["volume_change_fp64"] = a.total_volume() / v0 - 1.0
+    traj["energy"] = abs(b.energy() / a.energy() - 1.0)
+    out["trajectory"] = traj
+    out["reference"] = "the FP64 form of this library on the same input (equal to the FP64 oracle within 1e-12 per step)"
+    out["error_definition"] = "max over bubbles |mixed - fp64| / max |fp64| per row (positions, radii: their change)"
+    a.close()
+    b.close()
+    return out
+
+
+def run_gb300(args, world, rank, local):
+    import torch
+    import cubble_gb300 as cb
+    from cubble_gb300 import workloads
+    torch.cuda.set_device(local)
+    cb.build()
+    main = measure_form(args, world, rank, args.precision)
+    cfg, st, desc, r0, r1 = main["cfg"], main["st"], main["desc"], main["r0"], main["r1"]
+    value, el = main["value"], main["el"]
+    attempts = r1["attempts"] - r0["attempts"]
+    searches = r1["searches"] - r0["searches"]
 
     # end to end through the C ABI with pinned host buffers: upload, search +
     # bootstrap, K steps each returning its report to the host, download.
@@ -292,7 +378,6 @@ def run_gb300(args, world, rank, local):
     if not args.no_e2e:
         host, keep = pinned_copy(st)
         g2 = cb.GpuFoam(cfg)
-        out = {k: np.empty_like(v) for k, v in host.items()}
         barrier(world)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -317,7 +402,22 @@ def run_gb300(args, world, rank, local):
                "steps": nsteps, "note": "state upload, search, bootstrap, %d steps each reading "
                                          "its report back, state download" % nsteps}
         g2.close()
-        del keep, out
+        del keep
+
+    mixed = None
+    if args.precision == 0 and not args.no_mixed:
+        mx = measure_form(args, world, rank, 1, clocks_on=False)
+        mixed = {"value": mx["value"], "unit": "bubble-steps/s",
+                 "ms_per_step": 1e3 * mx["el"] / args.steps,
+                 "speedup_vs_fp64": mx["value"] / value,
+                 "attempts": mx["r1"]["attempts"] - mx["r0"]["attempts"],
+                 "searches": mx["r1"]["searches"] - mx["r0"]["searches"],
+                 "roofline": mx["roofline"], "gpu_launches": mx["launches"],
+                 "workload": "same foam, mixed precision: FP32 pair geometry on exact 64-bit "
+                             "fixed-point differences, FP32 rates; FP64 positions, radii, "
+                             "volume sum and fix, error norm, energy"}
+        if rank == 0:
+            mixed["error_vs_fp64"] = mixed_errors(args)
 
     base = None
     if rank == 0 and not args.no_cpu:
@@ -337,10 +437,10 @@ def run_gb300(args, world, rank, local):
                    "graph": bool(args.graph), "parallelism": "replicas" if world > 1 else "single foam",
                    "l2": "working set larger than L2 (state + pairs > 129 MB)",
                    "attempts": attempts, "searches": searches,
-                   "pairs_per_bubble": np_per_n, "bubbles_end": r1["count"],
+                   "pairs_per_bubble": main["np_per_n"], "bubbles_end": r1["count"],
                    "deleted": r1["deleted"] - r0["deleted"], "dt_end": r1["time_step"]},
-        "roofline": roof, "cpu_baseline": base, "e2e": e2e, "gpu_launches": launches,
-        "clocks": clk,
+        "roofline": main["roofline"], "cpu_baseline": base, "e2e": e2e,
+        "gpu_launches": main["launches"], "clocks": main["clocks"], "mixed": mixed,
     }
     print(json.dumps(line))
 
@@ -367,6 +467,7 @@ def main():
     ap.add_argument("--ref-steps", type=int, default=200)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

@@ -65,10 +65,12 @@ struct DevConst {
     double flow_lbb[3], flow_tfr[3], flow_vel[3];
     double wall_drag, min_rad, f0, K, kappa, skin, vol_mul_const, ain, tol;
     double half_iv[3];
-    // Mixed form: 32-bit fixed-point coordinates q = x * fx_scale + fx_off
-    // (mod 2^32 on periodic axes, so q_i - q_j is the minimum image), and
-    // fx_inv converts a q difference back to length units.
-    double fx_scale[3], fx_off[3];
+    // Mixed form: 64-bit fixed-point coordinates
+    //   q = (int64)round(x * fx_scale + fx_off) << fx_shift
+    // (mod 2^64 on periodic axes, so q_i - q_j is the minimum image);
+    // fx_unit converts a length to q units, fx_inv a q difference back.
+    double fx_scale[3], fx_off[3], fx_unit[3];
+    int fx_shift[3];
     float fx_inv[3];
     int mixed;
     float pre_margin;  // FP32 pair-search prefilter margin (length units)

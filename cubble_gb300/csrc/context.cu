@@ -147,17 +147,24 @@ void fill_const(cb_context *c) {
     k.mixed = f.precision == CB_PRECISION_MIXED ? 1 : 0;
     for (int a = 0; a < 3; a++) {
         const double iv = k.iv[a];
-        if (iv <= 0.0) {
-            k.fx_scale[a] = k.fx_off[a] = 0.0;
-            k.fx_inv[a] = 0.f;
-        } else if (!k.wall[a]) {  // q = (x - lbb) 2^32 / L, wraps mod 2^32
-            k.fx_scale[a] = 4294967296.0 / iv;
+        k.fx_scale[a] = k.fx_off[a] = k.fx_unit[a] = 0.0;
+        k.fx_shift[a] = 0;
+        k.fx_inv[a] = 0.f;
+        if (iv <= 0.0) continue;
+        if (!k.wall[a]) {
+            // (x - lbb) 2^62 / L fits int64 for x within two boxes of the
+            // box; << 2 maps the box onto 2^64, so differences wrap to the
+            // minimum image
+            k.fx_scale[a] = 4611686018427387904.0 / iv;
             k.fx_off[a] = -k.lbb[a] * k.fx_scale[a];
-            k.fx_inv[a] = (float)(iv / 4294967296.0);
-        } else {  // q = (x - lbb + L/4) 2^30 / (1.5 L), no wrap
-            k.fx_scale[a] = 1073741824.0 / (1.5 * iv);
+            k.fx_shift[a] = 2;
+            k.fx_unit[a] = 18446744073709551616.0 / iv;
+            k.fx_inv[a] = (float)(iv / 18446744073709551616.0);
+        } else {  // (x - lbb + L/4) 2^61 / (1.5 L), no wrap
+            k.fx_scale[a] = 2305843009213693952.0 / (1.5 * iv);
             k.fx_off[a] = -(k.lbb[a] - 0.25 * iv) * k.fx_scale[a];
-            k.fx_inv[a] = (float)(1.5 * iv / 1073741824.0);
+            k.fx_unit[a] = k.fx_scale[a];
+            k.fx_inv[a] = (float)(1.5 * iv / 2305843009213693952.0);
         }
     }
     // FP32 coordinates carry |x| 2^-24 rounding; 1e-5 (maxabs + interval) is

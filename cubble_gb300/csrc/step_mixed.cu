@@ -8,15 +8,17 @@
 //   * FP32: velocities and radius rates (the dxdt / dxdto / dxdtp rows hold
 //     floats), the pair geometry, overlap velocities, overlap areas and the
 //     gas flux, the mean-field arithmetic per bubble;
-//   * pair geometry works on exact differences of 32-bit fixed-point
-//     coordinates: q = x * 2^32 / L (mod 2^32) on a periodic axis, so the
+//   * pair geometry works on exact differences of 64-bit fixed-point
+//     coordinates: q = x * 2^64 / L (mod 2^64) on a periodic axis, so the
 //     integer difference q_i - q_j wraps to the minimum image by itself
 //     (wrappedDifference, src/kernels.cu:1094-1114, becomes one integer
-//     subtraction) and carries L / 2^32 absolute resolution; on a wall axis
-//     q = (x - lbb + L / 4) * 2^30 / (1.5 L) without wrapping.
-// The packed predicted state is 16 bytes per bubble (q_x, q_y, q_z, r_p in
-// 3D; q_x, q_y, r_p, 1/r_p in 2D) and the pair kernel adds its results with
-// 16-byte vector FP32 reductions.
+//     subtraction) and is exact at any separation, also for nearly
+//     coincident bubbles; on a wall axis q = (x - lbb + L/4) 2^61 / (1.5 L)
+//     without wrapping. Only the conversion of the exact difference to FP32
+//     rounds (relative 2^-24).
+// The packed predicted state is 32 bytes per bubble (q_x, q_y, q_z, r_p,
+// 1/r_p) and the pair kernel adds its results with 16-byte vector FP32
+// reductions.
 #include "common.cuh"
 
 namespace cbg {
@@ -43,12 +45,44 @@ __device__ __forceinline__ void red_add4(float4 *p, float a, float b, float c, f
                  : "memory");
 }
 
-__device__ __forceinline__ unsigned int fixq(const DevConst &k, int a, double x) {
-    return (unsigned int)(unsigned long long)__double2ll_rn(fma(x, k.fx_scale[a], k.fx_off[a]));
+// Predicted state of one bubble in the mixed form (32 bytes).
+struct __align__(16) PredMx {
+    unsigned long long q[3];
+    float r, inv;
+};
+
+__device__ __forceinline__ unsigned long long fixq(const DevConst &k, int a, double x) {
+    return (unsigned long long)__double2ll_rn(fma(x, k.fx_scale[a], k.fx_off[a]))
+           << k.fx_shift[a];
 }
 
-__device__ __forceinline__ float qdiff(unsigned int qi, unsigned int qj, float inv) {
-    return (float)(int)(qi - qj) * inv;
+// Adds a length increment (FP32) to a fixed-point coordinate.
+__device__ __forceinline__ unsigned long long fixadd(unsigned long long q, float inc, float unit) {
+    return q + (unsigned long long)__float2ll_rn(inc * unit);
+}
+
+__device__ __forceinline__ float qdiff(unsigned long long qi, unsigned long long qj, float inv) {
+    return (float)(long long)(qi - qj) * inv;
+}
+
+__device__ __forceinline__ PredMx ld_pred(const Bufs &b, int i) {
+    const int4 *p = reinterpret_cast<const int4 *>(b.pred) + 2 * (size_t)i;
+    const int4 u = p[0], v = p[1];
+    PredMx r;
+    r.q[0] = (unsigned long long)(unsigned)u.x | ((unsigned long long)(unsigned)u.y << 32);
+    r.q[1] = (unsigned long long)(unsigned)u.z | ((unsigned long long)(unsigned)u.w << 32);
+    r.q[2] = (unsigned long long)(unsigned)v.x | ((unsigned long long)(unsigned)v.y << 32);
+    r.r = __int_as_float(v.z);
+    r.inv = __int_as_float(v.w);
+    return r;
+}
+
+__device__ __forceinline__ void st_pred(const Bufs &b, int i, const PredMx &r) {
+    int4 *p = reinterpret_cast<int4 *>(b.pred) + 2 * (size_t)i;
+    p[0] = make_int4((int)(unsigned)r.q[0], (int)(unsigned)(r.q[0] >> 32), (int)(unsigned)r.q[1],
+                     (int)(unsigned)(r.q[1] >> 32));
+    p[1] = make_int4((int)(unsigned)r.q[2], (int)(unsigned)(r.q[2] >> 32), __float_as_int(r.r),
+                     __float_as_int(r.inv));
 }
 
 // ---------------------------------------------------------------- predict
@@ -66,26 +100,19 @@ __global__ void __launch_bounds__(kBlock) k_predict_mx(Bufs b) {
                 *V3 = frow(b, c, RV3);
     const float *O0 = frow(b, c, RVO0), *O1 = frow(b, c, RVO1), *O2 = frow(b, c, RVO2),
                 *O3 = frow(b, c, RVO3);
-    const float s0 = (float)k.fx_scale[0], s1 = (float)k.fx_scale[1], s2 = (float)k.fx_scale[2];
+    const float u0 = (float)k.fx_unit[0], u1 = (float)k.fx_unit[1], u2 = (float)k.fx_unit[2];
     float sA = 0.f, sAr = 0.f;
-    int4 *P = reinterpret_cast<int4 *>(b.pred);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         // AB2 increment h (3 v - vo) in FP32, added to the exact fixed point of x
-        const unsigned int qx = fixq(k, 0, X[i]) + __float2int_rn(h * fmaf(3.f, V0[i], -O0[i]) * s0);
-        const unsigned int qy = fixq(k, 1, Y[i]) + __float2int_rn(h * fmaf(3.f, V1[i], -O1[i]) * s1);
+        PredMx p;
+        p.q[0] = fixadd(fixq(k, 0, X[i]), h * fmaf(3.f, V0[i], -O0[i]), u0);
+        p.q[1] = fixadd(fixq(k, 1, Y[i]), h * fmaf(3.f, V1[i], -O1[i]), u1);
+        p.q[2] = DIM == 3 ? fixadd(fixq(k, 2, Z[i]), h * fmaf(3.f, V2[i], -O2[i]), u2) : 0ull;
         float rp = (float)R[i];
         if (gas) rp = fmaf(h, fmaf(3.f, V3[i], -O3[i]), rp);
-        int4 p;
-        p.x = (int)qx;
-        p.y = (int)qy;
-        if (DIM == 3) {
-            p.z = (int)(fixq(k, 2, Z[i]) + __float2int_rn(h * fmaf(3.f, V2[i], -O2[i]) * s2));
-            p.w = __float_as_int(rp);
-        } else {
-            p.z = __float_as_int(rp);
-            p.w = __float_as_int(1.f / rp);
-        }
-        P[i] = p;
+        p.r = rp;
+        p.inv = 1.f / rp;
+        st_pred(b, i, p);
         if (gas) {
             const float apr = DIM == 3 ? (4.f * (float)kPi) * rp : 2.f * (float)kPi;
             sA = fmaf(apr, rp, sA);
@@ -120,7 +147,6 @@ __global__ void __launch_bounds__(kBlock) k_pairs_mx(Bufs b) {
     const int *PI = b.ps[c->prole[PI0]];
     const int *PJ = b.ps[c->prole[PJ0]];
     const float *V0 = frow(b, c, RV0), *V1 = frow(b, c, RV1), *V2 = frow(b, c, RV2);
-    const int4 *P = reinterpret_cast<const int4 *>(b.pred);
     float4 *AV = acc_v(b);
     float *AO = acc_ov(b, cap);
     float4 *AF = acc_fl(b, cap);
@@ -131,12 +157,11 @@ __global__ void __launch_bounds__(kBlock) k_pairs_mx(Bufs b) {
         const int i = PI[p], j = PJ[p];
         if (FLOW)  // src/kernels.cu:191-207 (added for every pair)
             red_add4(AF + j, V0[i], V1[i], DIM == 3 ? V2[i] : 0.f, 0.f);
-        const int4 a = P[i], q = P[j];
-        const float dx = qdiff((unsigned)a.x, (unsigned)q.x, ix);
-        const float dy = qdiff((unsigned)a.y, (unsigned)q.y, iy);
-        const float dz = DIM == 3 ? qdiff((unsigned)a.z, (unsigned)q.z, iz) : 0.f;
-        const float r1 = __int_as_float(DIM == 3 ? a.w : a.z);
-        const float r2 = __int_as_float(DIM == 3 ? q.w : q.z);
+        const PredMx a = ld_pred(b, i), q = ld_pred(b, j);
+        const float dx = qdiff(a.q[0], q.q[0], ix);
+        const float dy = qdiff(a.q[1], q.q[1], iy);
+        const float dz = DIM == 3 ? qdiff(a.q[2], q.q[2], iz) : 0.f;
+        const float r1 = a.r, r2 = q.r;
         float m = dx * dx;
         m = fmaf(dy, dy, m);
         if (DIM == 3) m = fmaf(dz, dz, m);
@@ -156,8 +181,7 @@ __global__ void __launch_bounds__(kBlock) k_pairs_mx(Bufs b) {
                     oa = fabsf(r2sq - (t * t) * (rs * rs));
                     oa = DIM == 3 ? oa * (float)kPi : 2.f * sqrtf(oa);
                 }
-                const float inv1 = DIM == 3 ? __fdividef(1.f, r1) : __int_as_float(a.w);
-                const float inv2 = DIM == 3 ? __fdividef(1.f, r2) : __int_as_float(q.w);
+                const float inv1 = a.inv, inv2 = q.inv;
                 g = oa * (inv2 - inv1);
                 atomicAdd(AO + i, oa);
                 atomicAdd(AO + j, oa);
@@ -403,34 +427,27 @@ __global__ void __launch_bounds__(kBlock) k_boot_mx(Bufs b, int phase) {
     float *O0 = frow(b, c, RVO0), *O1 = frow(b, c, RVO1), *O2 = frow(b, c, RVO2),
           *O3 = frow(b, c, RVO3);
     double *PATH = drow(b, c, RPATH);
-    int4 *P = reinterpret_cast<int4 *>(b.pred);
     float4 *AV = acc_v(b);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         if (phase == 0) {
-            const float r = (float)R[i];
-            int4 p;
-            p.x = (int)fixq(k, 0, X[i]);
-            p.y = (int)fixq(k, 1, Y[i]);
-            if (DIM == 3) {
-                p.z = (int)fixq(k, 2, Z[i]);
-                p.w = __float_as_int(r);
-            } else {
-                p.z = __float_as_int(r);
-                p.w = __float_as_int(1.f / r);
-            }
-            P[i] = p;
+            PredMx p;
+            p.q[0] = fixq(k, 0, X[i]);
+            p.q[1] = fixq(k, 1, Y[i]);
+            p.q[2] = DIM == 3 ? fixq(k, 2, Z[i]) : 0ull;
+            p.r = (float)R[i];
+            p.inv = 1.f / p.r;
+            st_pred(b, i, p);
             O0[i] = O1[i] = O2[i] = O3[i] = 0.f;
             PATH[i] = 0.0;
         } else {
             const float4 a = AV[i];
-            if (phase == 1) {
-                int4 p = P[i];
-                p.x = (int)((unsigned)p.x + (unsigned)__double2ll_rn((double)a.x * ts * k.fx_scale[0]));
-                p.y = (int)((unsigned)p.y + (unsigned)__double2ll_rn((double)a.y * ts * k.fx_scale[1]));
+            if (phase == 1) {  // euler, src/kernels.cu:959-969
+                PredMx p = ld_pred(b, i);
+                p.q[0] += (unsigned long long)__double2ll_rn((double)a.x * ts * k.fx_unit[0]);
+                p.q[1] += (unsigned long long)__double2ll_rn((double)a.y * ts * k.fx_unit[1]);
                 if (DIM == 3)
-                    p.z = (int)((unsigned)p.z +
-                                (unsigned)__double2ll_rn((double)a.z * ts * k.fx_scale[2]));
-                P[i] = p;
+                    p.q[2] += (unsigned long long)__double2ll_rn((double)a.z * ts * k.fx_unit[2]);
+                st_pred(b, i, p);
             } else {
                 O0[i] = a.x;
                 O1[i] = a.y;

@@ -1,0 +1,129 @@
+"""GPU: the mixed-precision form against the FP64 oracle on the same inputs.
+
+Errors are norm-wise: max |mixed - fp64| over bubbles divided by the largest
+|fp64| of the same row (for positions and radii, of their change in the
+step). Bars: 1e-6 per step for positions, velocities and radius rates in 3D
+(2e-6 for the 2D radius rate and 4e-6 for 2D overlap lengths, where the
+chord of nearly tangent circles is a square root of a small difference);
+total gas volume within 1e-10 of the FP64 run; pair sets, deletion sets and
+the compaction order bit-exact (they are computed from the FP64 positions).
+"""
+import math
+
+import numpy as np
+import pytest
+
+import cubble_gb300 as cb
+from cubble_gb300 import workloads
+from helpers import by_index, max_rel, pair_set
+
+pytestmark = pytest.mark.gpu
+
+
+def case(dim, n, **kw):
+    if dim == 3:
+        return workloads.foam(n, 3, 0.8, rstd=0.15, rclip=(0.3, 2.5), seed=41, **kw)
+    return workloads.foam(n, 2, 0.9, seed=42, min_rad=0.05, **kw)
+
+
+def prepared(oracle_mod, dim, n, steps=5):
+    cfg, st = case(dim, n)
+    o = oracle_mod.OracleFoam(cfg)
+    o.load_state(st)
+    workloads.prepare(o)
+    o.integrate(steps)
+    return cfg, o
+
+
+def mixed_from(o, dim, n, **kw):
+    cfg_m, _ = case(dim, n, precision=1, **kw)
+    g = cb.GpuFoam(cfg_m)
+    g.load_state(o.get_state())
+    i, j = o.pairs()
+    g.set_pairs(i, j)
+    g.set_time(o.report()["time_step"])
+    return g
+
+
+@pytest.mark.parametrize("dim", [3, 2])
+def test_mixed_single_attempt(oracle_mod, dim):
+    cfg, o = prepared(oracle_mod, dim, 8000)
+    s = o.get_state()
+    g = mixed_from(o, dim, 8000)
+    ag, ao = g.attempt(), o.attempt()
+    lim = 1e-6
+    for k, base in (("xp", "x"), ("yp", "y"), ("zp", "z"), ("rp", "r")):
+        if dim == 2 and k == "zp":
+            continue
+        assert max_rel(ag[k] - s[base], ao[k] - s[base]) <= lim, k
+    for k in ("dxdtp", "dydtp", "dzdtp"):
+        if dim == 2 and k == "dzdtp":
+            continue
+        assert max_rel(ag[k], ao[k]) <= lim, k
+    assert max_rel(ag["drdtp"], ao["drdtp"]) <= (lim if dim == 3 else 2e-6)
+    assert max_rel(ag["overlap"], ao["overlap"]) <= (lim if dim == 3 else 4e-6)
+    assert max_rel(ag["path_new"], ao["path_new"]) <= lim
+    for k in ("total_area", "total_area_per_radius", "total_overlap_area",
+              "total_overlap_area_per_radius"):
+        assert ag[k] == pytest.approx(ao[k], rel=lim), k
+    assert np.array_equal(ag["delete_flags"], ao["delete_flags"])
+
+
+@pytest.mark.parametrize("graph", [0, 1])
+@pytest.mark.parametrize("dim", [3, 2])
+def test_mixed_trajectory(oracle_mod, dim, graph):
+    cfg, o = prepared(oracle_mod, dim, 8000)
+    s0 = by_index(o.get_state())
+    g = mixed_from(o, dim, 8000, use_graph=graph)
+    rg, ro = g.integrate(60), o.integrate(60)
+    for k in ("steps", "attempts", "searches", "deleted", "count", "num_pairs"):
+        assert rg[k] == ro[k], k
+    sg, so = by_index(g.get_state()), by_index(o.get_state())
+    for k in ("x", "y", "z"):
+        if dim == 2 and k == "z":
+            continue
+        assert max_rel(sg[k] - s0[k], so[k] - s0[k]) <= 1e-6, k
+    assert max_rel(sg["r"], so["r"]) <= 1e-8
+    assert g.total_volume() == pytest.approx(o.total_volume(), rel=1e-10)
+    assert g.energy() == pytest.approx(o.energy(), rel=1e-6)
+    gi, gj = g.pairs()
+    oi, oj = o.pairs()
+    assert pair_set(gi, gj, g.get_state()["index"]) == pair_set(oi, oj, o.get_state()["index"])
+
+
+@pytest.mark.parametrize("dim", [3, 2])
+def test_mixed_deletion_and_volume_fix(oracle_mod, dim):
+    kw = dict(rstd=0.3, rclip=(0.01, 2.0), seed=43, min_rad=0.2)
+    cfg, st = workloads.foam(4000, dim, 0.85, **kw)
+    cfg_m, _ = workloads.foam(4000, dim, 0.85, precision=1, **kw)
+    o = oracle_mod.OracleFoam(cfg)
+    g = cb.GpuFoam(cfg_m)
+    for f in (o, g):
+        f.load_state(st)
+        workloads.prepare(f)
+    ro, rg = o.integrate(1), g.integrate(1)
+    assert ro["deleted"] > 0
+    for k in ("deleted", "count", "num_pairs"):
+        assert rg[k] == ro[k], k
+    sg, so = g.get_state(), o.get_state()
+    assert np.array_equal(sg["index"], so["index"])
+    M = cfg.bubble_volume_multiplier
+    target = math.pi * M ** 2 if dim == 2 else 4.0 / 3.0 * math.pi * M ** 3
+    assert g.total_volume() == pytest.approx(target, rel=1e-12)
+
+
+def test_mixed_search_is_exact(oracle_mod):
+    cfg, st = case(3, 6000)
+    cfg_m, _ = case(3, 6000, precision=1)
+    o = oracle_mod.OracleFoam(cfg)
+    g = cb.GpuFoam(cfg_m)
+    for f in (o, g):
+        f.load_state(st)
+        f.search_neighbors()
+    gi, gj = g.pairs()
+    oi, oj = o.pairs()
+    assert np.array_equal(gi, oi) and np.array_equal(gj, oj)
+    sg, so = g.get_state(), o.get_state()
+    for k in ("x", "y", "z", "r", "saved_x"):
+        assert np.array_equal(sg[k], so[k]), k
+    assert np.array_equal(sg["index"], so["index"])
