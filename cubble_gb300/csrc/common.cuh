@@ -65,13 +65,10 @@ struct DevConst {
     double flow_lbb[3], flow_tfr[3], flow_vel[3];
     double wall_drag, min_rad, f0, K, kappa, skin, vol_mul_const, ain, tol;
     double half_iv[3];
-    // Mixed form: 64-bit fixed-point coordinates
-    //   q = (int64)round(x * fx_scale + fx_off) << fx_shift
-    // (mod 2^64 on periodic axes, so q_i - q_j is the minimum image);
-    // fx_unit converts a length to q units, fx_inv a q difference back.
-    double fx_scale[3], fx_off[3], fx_unit[3];
-    int fx_shift[3];
-    float fx_inv[3];
+    // Mixed form: 64-bit fixed-point coordinates q = x * 2^40 (see
+    // step_mixed.cu); lq / hq are the periodic box length and half of it in
+    // those units.
+    long long lq[3], hq[3];
     int mixed;
     float pre_margin;  // FP32 pair-search prefilter margin (length units)
     float half_iv32[3];
@@ -402,7 +399,7 @@ void launch_boot(const Launch &l, const Bufs &b, int dim, int phase);
 // step_mixed.cu (mixed form)
 void launch_predict_mx(const Launch &l, const Bufs &b, int dim);
 void launch_pairs_mx(const Launch &l, const Bufs &b, int dim, int mode);
-void launch_correct_mx(const Launch &l, const Bufs &b, int dim);
+void launch_correct_mx(const Launch &l, const Bufs &b, int dim, int mode, bool walls);
 void launch_boot_mx(const Launch &l, const Bufs &b, int dim, int phase);
 void launch_energy(const Launch &l, const Bufs &b, int dim, int per_bubble);
 void launch_volume(const Launch &l, const Bufs &b, int dim);

@@ -146,26 +146,8 @@ void fill_const(cb_context *c) {
     }
     k.mixed = f.precision == CB_PRECISION_MIXED ? 1 : 0;
     for (int a = 0; a < 3; a++) {
-        const double iv = k.iv[a];
-        k.fx_scale[a] = k.fx_off[a] = k.fx_unit[a] = 0.0;
-        k.fx_shift[a] = 0;
-        k.fx_inv[a] = 0.f;
-        if (iv <= 0.0) continue;
-        if (!k.wall[a]) {
-            // (x - lbb) 2^62 / L fits int64 for x within two boxes of the
-            // box; << 2 maps the box onto 2^64, so differences wrap to the
-            // minimum image
-            k.fx_scale[a] = 4611686018427387904.0 / iv;
-            k.fx_off[a] = -k.lbb[a] * k.fx_scale[a];
-            k.fx_shift[a] = 2;
-            k.fx_unit[a] = 18446744073709551616.0 / iv;
-            k.fx_inv[a] = (float)(iv / 18446744073709551616.0);
-        } else {  // (x - lbb + L/4) 2^61 / (1.5 L), no wrap
-            k.fx_scale[a] = 2305843009213693952.0 / (1.5 * iv);
-            k.fx_off[a] = -(k.lbb[a] - 0.25 * iv) * k.fx_scale[a];
-            k.fx_unit[a] = k.fx_scale[a];
-            k.fx_inv[a] = (float)(1.5 * iv / 2305843009213693952.0);
-        }
+        k.lq[a] = (long long)std::llround(k.iv[a] * 1099511627776.0);  // 2^40
+        k.hq[a] = k.lq[a] / 2;
     }
     // FP32 coordinates carry |x| 2^-24 rounding; 1e-5 (maxabs + interval) is
     // more than 20x the worst error of the prefiltered distance.
@@ -185,7 +167,7 @@ void launch_attempt_kernels(const cb_context *c, const Launch &l, const Bufs &b,
     if (c->hk.mixed) {
         if (which & 1) launch_predict_mx(l, b, dim);
         if (which & 2) launch_pairs_mx(l, b, dim, c->mode());
-        if (which & 4) launch_correct_mx(l, b, dim);
+        if (which & 4) launch_correct_mx(l, b, dim, c->mode(), c->hk.any_wall != 0);
     } else {
         if (which & 1) launch_predict(l, b, dim);
         if (which & 2) launch_pairs(l, b, dim, c->mode());
@@ -367,6 +349,12 @@ int cb_create(const cb_config *cfg, cb_context **out) {
     if (cfg->capacity <= 0) return fail(CB_ERR_INVALID_ARGUMENT, "capacity must be positive");
     if ((long long)cfg->capacity * 2 + 64 > 0x7fffffffLL)
         return fail(CB_ERR_INVALID_ARGUMENT, "capacity too large");
+    if (cfg->precision == CB_PRECISION_MIXED) {
+        for (int a = 0; a < 3; a++)
+            if (std::fabs(cfg->lbb[a]) > 2097152.0 || std::fabs(cfg->tfr[a]) > 2097152.0)
+                return fail(CB_ERR_INVALID_ARGUMENT,
+                            "mixed precision needs box corners within +-2^21 (fixed point 2^40)");
+    }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1)
         return fail(CB_ERR_NO_DEVICE, "no CUDA device");

@@ -7,25 +7,104 @@
 //     sums, the energy;
 //   * FP32: velocities and radius rates (the dxdt / dxdto / dxdtp rows hold
 //     floats), the pair geometry, overlap velocities, overlap areas and the
-//     gas flux, the mean-field arithmetic per bubble;
-//   * pair geometry works on exact differences of 64-bit fixed-point
-//     coordinates: q = x * 2^64 / L (mod 2^64) on a periodic axis, so the
-//     integer difference q_i - q_j wraps to the minimum image by itself
-//     (wrappedDifference, src/kernels.cu:1094-1114, becomes one integer
-//     subtraction) and is exact at any separation, also for nearly
-//     coincident bubbles; on a wall axis q = (x - lbb + L/4) 2^61 / (1.5 L)
-//     without wrapping. Only the conversion of the exact difference to FP32
-//     rounds (relative 2^-24).
-// The packed predicted state is 32 bytes per bubble (q_x, q_y, q_z, r_p,
-// 1/r_p) and the pair kernel adds its results with 16-byte vector FP32
-// reductions.
+//     gas flux, the mean-field arithmetic per bubble, the expansion since the
+//     last search (from the FP64 difference to the saved position).
+//
+// GB300 runs FP64 arithmetic *and* every 64-bit conversion (double <-> int64,
+// float <-> double, int64 -> float) on one unit at 1/64 of the FP32 rate.
+// The mixed kernels therefore convert on the integer pipe, from the IEEE-754
+// bit patterns (fix_from_double, fix_from_float, double_from_float,
+// float_from_double below), and use FP64 arithmetic only for the position,
+// radius and path updates, the differences to the saved position and the
+// volume sum (12 FP64 instructions per bubble in 3D).
+//
+// Pair geometry works on exact differences of 64-bit fixed-point coordinates
+// q = x * 2^40 (|x| < 2^21): the integer difference q_i - q_j is exact at any
+// separation (also for nearly coincident bubbles); the minimum image on a
+// periodic axis is an integer compare against half the box
+// (wrappedDifference, src/kernels.cu:1094-1114). Only the final conversion of
+// the difference to FP32 rounds (relative 2^-24). The packed predicted state
+// is 32 bytes per bubble (q_x, q_y, q_z, r_p, 1/r_p) and the pair kernel adds
+// its results with 16-byte vector FP32 reductions.
 #include "common.cuh"
 
 namespace cbg {
 namespace {
 
+constexpr int kFixBits = 40;
+constexpr float kFixInv = 9.094947017729282e-13f;  // 2^-40
+
 __device__ __forceinline__ float *frow(const Bufs &b, const Ctrl *c, int role) {
     return reinterpret_cast<float *>(b.ds[c->drole[role]]);
+}
+
+// ------------------------------------------------- integer-pipe conversions
+// x * 2^40 rounded toward zero, from the bits of x (|x| < 2^23).
+__device__ __forceinline__ long long fix_from_double(double x) {
+    const long long b = __double_as_longlong(x);
+    const int e = (int)(((unsigned long long)b >> 52) & 0x7ff);
+    const long long m = (b & 0x000fffffffffffffLL) | 0x0010000000000000LL;
+    const int sh = e - (1075 - kFixBits);  // x = m 2^(e - 1075)
+    long long q = sh >= 0 ? (m << min(sh, 10)) : (sh > -64 ? (m >> -sh) : 0LL);
+    if (e == 0) q = 0;
+    return b < 0 ? -q : q;
+}
+
+// f * 2^40 rounded toward zero, from the bits of f (|f| < 2^23).
+__device__ __forceinline__ long long fix_from_float(float f) {
+    const int b = __float_as_int(f);
+    const int e = (b >> 23) & 0xff;
+    const long long m = (long long)((b & 0x7fffff) | 0x800000);
+    const int sh = e - (150 - kFixBits);  // f = m 2^(e - 150)
+    long long q = sh >= 0 ? (m << min(sh, 39)) : (sh > -64 ? (m >> -sh) : 0LL);
+    if (e == 0) q = 0;
+    return b < 0 ? -q : q;
+}
+
+// A fixed-point difference in length units as FP32: |d| = hi 2^32 + lo with
+// two 32-bit conversions (the 64-bit one would take the FP64 unit).
+__device__ __forceinline__ float len_from_fix(long long d) {
+    const unsigned long long a = (unsigned long long)(d < 0 ? -d : d);
+    const float f = fmaf(__uint2float_rn((unsigned int)(a >> 32)), 4294967296.f,
+                         __uint2float_rn((unsigned int)a));
+    return (d < 0 ? -f : f) * kFixInv;
+}
+
+// Exact float -> double from the bits (FP32 subnormals become 0).
+__device__ __forceinline__ double double_from_float(float f) {
+    const unsigned int b = __float_as_uint(f);
+    const unsigned int e = (b >> 23) & 0xffu;
+    const unsigned long long s = (unsigned long long)(b >> 31) << 63;
+    if (e == 0) return __longlong_as_double((long long)s);
+    const unsigned long long de = e == 0xffu ? 0x7ffull : (unsigned long long)(e + 896u);
+    return __longlong_as_double(
+        (long long)(s | (de << 52) | ((unsigned long long)(b & 0x7fffffu) << 29)));
+}
+
+// double -> float rounded toward zero, from the bits.
+__device__ __forceinline__ float float_from_double(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ff);
+    const unsigned int s = (unsigned int)(b >> 63) << 31;
+    const unsigned int man = (unsigned int)((b >> 29) & 0x7fffffull);
+    const int fe = e - 896;
+    unsigned int bits;
+    if (e == 0x7ff)
+        bits = s | 0x7f800000u | man | ((b & 0xfffffffffffffull) ? 0x400000u : 0u);
+    else if (fe <= 0)
+        bits = s;
+    else if (fe >= 255)
+        bits = s | 0x7f800000u;
+    else
+        bits = s | ((unsigned int)fe << 23) | man;
+    return __uint_as_float(bits);
+}
+
+// Minimum image of a fixed-point difference on a periodic axis.
+__device__ __forceinline__ long long wrap_fix(long long d, long long half, long long len) {
+    if (d > half) d -= len;
+    else if (d < -half) d += len;
+    return d;
 }
 
 // Accumulator layout of the mixed form inside `acc` (64 bytes per bubble):
@@ -47,42 +126,27 @@ __device__ __forceinline__ void red_add4(float4 *p, float a, float b, float c, f
 
 // Predicted state of one bubble in the mixed form (32 bytes).
 struct __align__(16) PredMx {
-    unsigned long long q[3];
+    long long q[3];
     float r, inv;
 };
 
-__device__ __forceinline__ unsigned long long fixq(const DevConst &k, int a, double x) {
-    return (unsigned long long)__double2ll_rn(fma(x, k.fx_scale[a], k.fx_off[a]))
-           << k.fx_shift[a];
-}
-
-// Adds a length increment (FP32) to a fixed-point coordinate.
-__device__ __forceinline__ unsigned long long fixadd(unsigned long long q, float inc, float unit) {
-    return q + (unsigned long long)__float2ll_rn(inc * unit);
-}
-
-__device__ __forceinline__ float qdiff(unsigned long long qi, unsigned long long qj, float inv) {
-    return (float)(long long)(qi - qj) * inv;
-}
-
 __device__ __forceinline__ PredMx ld_pred(const Bufs &b, int i) {
-    const int4 *p = reinterpret_cast<const int4 *>(b.pred) + 2 * (size_t)i;
-    const int4 u = p[0], v = p[1];
+    const longlong2 *p = reinterpret_cast<const longlong2 *>(b.pred) + 2 * (size_t)i;
+    const longlong2 u = p[0], v = p[1];
     PredMx r;
-    r.q[0] = (unsigned long long)(unsigned)u.x | ((unsigned long long)(unsigned)u.y << 32);
-    r.q[1] = (unsigned long long)(unsigned)u.z | ((unsigned long long)(unsigned)u.w << 32);
-    r.q[2] = (unsigned long long)(unsigned)v.x | ((unsigned long long)(unsigned)v.y << 32);
-    r.r = __int_as_float(v.z);
-    r.inv = __int_as_float(v.w);
+    r.q[0] = u.x;
+    r.q[1] = u.y;
+    r.q[2] = v.x;
+    r.r = __int_as_float((int)(v.y & 0xffffffffLL));
+    r.inv = __int_as_float((int)(v.y >> 32));
     return r;
 }
 
 __device__ __forceinline__ void st_pred(const Bufs &b, int i, const PredMx &r) {
-    int4 *p = reinterpret_cast<int4 *>(b.pred) + 2 * (size_t)i;
-    p[0] = make_int4((int)(unsigned)r.q[0], (int)(unsigned)(r.q[0] >> 32), (int)(unsigned)r.q[1],
-                     (int)(unsigned)(r.q[1] >> 32));
-    p[1] = make_int4((int)(unsigned)r.q[2], (int)(unsigned)(r.q[2] >> 32), __float_as_int(r.r),
-                     __float_as_int(r.inv));
+    longlong2 *p = reinterpret_cast<longlong2 *>(b.pred) + 2 * (size_t)i;
+    p[0] = make_longlong2(r.q[0], r.q[1]);
+    p[1] = make_longlong2(r.q[2], (long long)(unsigned int)__float_as_int(r.r) |
+                                      ((long long)__float_as_int(r.inv) << 32));
 }
 
 // ---------------------------------------------------------------- predict
@@ -90,7 +154,6 @@ template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_predict_mx(Bufs b) {
     __shared__ double smem[32];
     const Ctrl *c = b.ctrl;
-    const DevConst &k = *b.k;
     const int n = c->n;
     const float h = (float)(0.5 * c->dt);
     const int gas = c->use_gas;
@@ -100,15 +163,15 @@ __global__ void __launch_bounds__(kBlock) k_predict_mx(Bufs b) {
                 *V3 = frow(b, c, RV3);
     const float *O0 = frow(b, c, RVO0), *O1 = frow(b, c, RVO1), *O2 = frow(b, c, RVO2),
                 *O3 = frow(b, c, RVO3);
-    const float u0 = (float)k.fx_unit[0], u1 = (float)k.fx_unit[1], u2 = (float)k.fx_unit[2];
     float sA = 0.f, sAr = 0.f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        // AB2 increment h (3 v - vo) in FP32, added to the exact fixed point of x
+        // AB2 increment h (3 v - vo) in FP32 on the fixed point of x
         PredMx p;
-        p.q[0] = fixadd(fixq(k, 0, X[i]), h * fmaf(3.f, V0[i], -O0[i]), u0);
-        p.q[1] = fixadd(fixq(k, 1, Y[i]), h * fmaf(3.f, V1[i], -O1[i]), u1);
-        p.q[2] = DIM == 3 ? fixadd(fixq(k, 2, Z[i]), h * fmaf(3.f, V2[i], -O2[i]), u2) : 0ull;
-        float rp = (float)R[i];
+        p.q[0] = fix_from_double(X[i]) + fix_from_float(h * fmaf(3.f, V0[i], -O0[i]));
+        p.q[1] = fix_from_double(Y[i]) + fix_from_float(h * fmaf(3.f, V1[i], -O1[i]));
+        p.q[2] = DIM == 3 ? fix_from_double(Z[i]) + fix_from_float(h * fmaf(3.f, V2[i], -O2[i]))
+                          : 0LL;
+        float rp = float_from_double(R[i]);
         if (gas) rp = fmaf(h, fmaf(3.f, V3[i], -O3[i]), rp);
         p.r = rp;
         p.inv = 1.f / rp;
@@ -119,8 +182,8 @@ __global__ void __launch_bounds__(kBlock) k_predict_mx(Bufs b) {
             sAr += apr;
         }
     }
-    const double tA = block_reduce((double)sA, OpSum(), smem);
-    const double tAr = block_reduce((double)sAr, OpSum(), smem);
+    const double tA = block_reduce(double_from_float(sA), OpSum(), smem);
+    const double tAr = block_reduce(double_from_float(sAr), OpSum(), smem);
     if (threadIdx.x == 0) {
         b.part[0 * gridDim.x + blockIdx.x] = tA;
         b.part[1 * gridDim.x + blockIdx.x] = tAr;
@@ -151,27 +214,36 @@ __global__ void __launch_bounds__(kBlock) k_pairs_mx(Bufs b) {
     float *AO = acc_ov(b, cap);
     float4 *AF = acc_fl(b, cap);
     const float f0 = (float)k.f0;
-    const float ix = k.fx_inv[0], iy = k.fx_inv[1], iz = k.fx_inv[2];
+    const bool px = !k.wall[0], py = !k.wall[1], pz = DIM == 3 && !k.wall[2];
+    const long long hx = k.hq[0], hy = k.hq[1], hz = k.hq[2];
+    const long long lx = k.lq[0], ly = k.lq[1], lz = k.lq[2];
     float sAo = 0.f, sAor = 0.f;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
         const int i = PI[p], j = PJ[p];
         if (FLOW)  // src/kernels.cu:191-207 (added for every pair)
             red_add4(AF + j, V0[i], V1[i], DIM == 3 ? V2[i] : 0.f, 0.f);
         const PredMx a = ld_pred(b, i), q = ld_pred(b, j);
-        const float dx = qdiff(a.q[0], q.q[0], ix);
-        const float dy = qdiff(a.q[1], q.q[1], iy);
-        const float dz = DIM == 3 ? qdiff(a.q[2], q.q[2], iz) : 0.f;
+        long long ex = a.q[0] - q.q[0], ey = a.q[1] - q.q[1], ez = 0;
+        if (px) ex = wrap_fix(ex, hx, lx);
+        if (py) ey = wrap_fix(ey, hy, ly);
+        if (DIM == 3) {
+            ez = a.q[2] - q.q[2];
+            if (pz) ez = wrap_fix(ez, hz, lz);
+        }
+        const float dx = len_from_fix(ex), dy = len_from_fix(ey);
+        const float dz = DIM == 3 ? len_from_fix(ez) : 0.f;
         const float r1 = a.r, r2 = q.r;
         float m = dx * dx;
         m = fmaf(dy, dy, m);
         if (DIM == 3) m = fmaf(dz, dz, m);
         const float radii = r1 + r2;
         if (radii * radii >= m) {
+            // velocity f0 d (1/|d| - 1/(r1 + r2)), src/kernels.cu:218-233
             const float rs = rsqrtf(m);
             const float s = f0 * (rs - __fdividef(1.f, radii));
             const float fx = dx * s, fy = dy * s, fz = dz * s;
             float g = 0.f;
-            if (GAS) {
+            if (GAS) {  // pairwise gas exchange, src/kernels.cu:236-280
                 const float r1sq = r1 * r1, r2sq = r2 * r2;
                 float oa;
                 if (m < r1sq || m < r2sq) {
@@ -181,12 +253,11 @@ __global__ void __launch_bounds__(kBlock) k_pairs_mx(Bufs b) {
                     oa = fabsf(r2sq - (t * t) * (rs * rs));
                     oa = DIM == 3 ? oa * (float)kPi : 2.f * sqrtf(oa);
                 }
-                const float inv1 = a.inv, inv2 = q.inv;
-                g = oa * (inv2 - inv1);
+                g = oa * (q.inv - a.inv);
                 atomicAdd(AO + i, oa);
                 atomicAdd(AO + j, oa);
                 sAo += oa;
-                sAor = fmaf(oa, inv1 + inv2, sAor);
+                sAor = fmaf(oa, a.inv + q.inv, sAor);
             }
             red_add4(AV + i, fx, fy, fz, g);
             red_add4(AV + j, -fx, -fy, -fz, -g);
@@ -194,8 +265,8 @@ __global__ void __launch_bounds__(kBlock) k_pairs_mx(Bufs b) {
                 red_add4(AF + i, V0[j], V1[j], DIM == 3 ? V2[j] : 0.f, 0.f);
         }
     }
-    const double tAo = block_reduce((double)sAo, OpSum(), smem);
-    const double tAor = block_reduce((double)sAor, OpSum(), smem);
+    const double tAo = block_reduce(double_from_float(sAo), OpSum(), smem);
+    const double tAor = block_reduce(double_from_float(sAor), OpSum(), smem);
     if (threadIdx.x == 0) {
         b.part[2 * gridDim.x + blockIdx.x] = tAo;
         b.part[3 * gridDim.x + blockIdx.x] = tAor;
@@ -212,7 +283,7 @@ __global__ void __launch_bounds__(kBlock) k_pairs_mx(Bufs b) {
 }
 
 // ---------------------------------------------------------------- correct
-// touchesWall, src/kernels.cu:553-566 (FP32; x is the predicted coordinate)
+// touchesWall, src/kernels.cu:553-566, on FP32 distances to both walls.
 __device__ __forceinline__ bool touches_wall_f(float f0, float rad, float d1, float d2,
                                                float &velocity) {
     d1 = d1 * d1 < d2 * d2 ? d1 : d2;
@@ -225,17 +296,16 @@ __device__ __forceinline__ bool touches_wall_f(float f0, float rad, float d1, fl
     return false;
 }
 
-template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_correct_mx(Bufs b) {
+template <int DIM, bool GAS, bool FLOW, bool WALLS>
+__global__ void __launch_bounds__(kBlock, 2) k_correct_mx(Bufs b) {
     __shared__ double smem[32];
     __shared__ int ismem[32];
     Ctrl *c = b.ctrl;
     const DevConst &k = *b.k;
     const int n = c->n;
     const int cap = k.cap;
-    const double h64 = 0.5 * c->dt;
-    const float h = (float)h64;
-    const int gas = c->use_gas, flow = c->use_flow, path = c->inc_path;
+    const float h = (float)(0.5 * c->dt);
+    const int path = c->inc_path;
     const double *X = drow(b, c, RX), *Y = drow(b, c, RY), *Z = drow(b, c, RZ),
                  *R = drow(b, c, RR);
     double *XN = drow(b, c, RXN), *YN = drow(b, c, RYN), *ZN = drow(b, c, RZN),
@@ -250,7 +320,6 @@ __global__ void __launch_bounds__(kBlock) k_correct_mx(Bufs b) {
                  *S3 = drow(b, c, RS3);
     const double *PATH = drow(b, c, RPATH);
     double *PATHN = drow(b, c, RPATHN), *ERR = drow(b, c, RERR);
-    const int *NN = irow(b, c, INN);
     float4 *AV = acc_v(b);
     float *AO = acc_ov(b, cap);
     float4 *AF = acc_fl(b, cap);
@@ -259,8 +328,7 @@ __global__ void __launch_bounds__(kBlock) k_correct_mx(Bufs b) {
     const float mfa = (float)((sAr - sAor) / (sA - sAo));
     const float mfb = (float)(k.kappa * k.ain * (double)n / sA);
     const float kq = (float)(DIM == 3 ? k.K / (4.0 * kPi) : k.K / (2.0 * kPi));
-    const float f0 = (float)k.f0;
-    const float drag = (float)(1.0 - k.wall_drag);
+    const long long minr = __double_as_longlong(k.min_rad);
     long long merr = 0, mrad = 0;
     float mexp = 0.f;
     double vol = 0.0;
@@ -272,105 +340,105 @@ __global__ void __launch_bounds__(kBlock) k_correct_mx(Bufs b) {
         const float ox = O0[i], oy = O1[i], oz = DIM == 3 ? O2[i] : 0.f;
         const double x0 = X[i], y0 = Y[i], z0 = DIM == 3 ? Z[i] : 0.0, r0 = R[i];
         float vr = 0.f, or_ = 0.f;
-        float rp = (float)r0;
-        if (gas) {
+        float rp = float_from_double(r0);
+        if (GAS) {
             vr = V3[i];
             or_ = O3[i];
             rp = fmaf(h, fmaf(3.f, vr, -or_), rp);  // as k_predict_mx
         }
-        if (flow || k.any_wall) {
-            // predicted coordinates relative to the box corner (FP32)
+        if (FLOW || WALLS) {
+            // predicted coordinates as x0 + e (e the FP32 AB2 increment)
             const float ex = h * fmaf(3.f, vx, -ox), ey = h * fmaf(3.f, vy, -oy),
                         ez = h * fmaf(3.f, vz, -oz);
-            if (flow) {  // addFlowVelocity, src/kernels.cu:497-544
+            const float f0 = (float)k.f0;
+            if (FLOW) {  // addFlowVelocity, src/kernels.cu:497-544
                 const float4 fl = AF[i];
-                float multiplier = (float)NN[i];
+                float multiplier = (float)irow(b, c, INN)[i];
                 multiplier = multiplier > 0.f ? 1.f / multiplier : 0.f;
                 const float riSq = rp * rp;
-                const float lx = (float)(k.flow_lbb[0] - x0) - ex, tx = (float)(k.flow_tfr[0] - x0) - ex;
-                const float ly = (float)(k.flow_lbb[1] - y0) - ey, ty = (float)(k.flow_tfr[1] - y0) - ey;
+                const float lx = float_from_double(k.flow_lbb[0] - x0) - ex;
+                const float tx = float_from_double(k.flow_tfr[0] - x0) - ex;
+                const float ly = float_from_double(k.flow_lbb[1] - y0) - ey;
+                const float ty = float_from_double(k.flow_tfr[1] - y0) - ey;
                 int inside = (int)((tx > 0.f && lx < 0.f) || lx * lx <= riSq || tx * tx <= riSq);
                 inside *= (int)((ty > 0.f && ly < 0.f) || ly * ly <= riSq || ty * ty <= riSq);
                 if (DIM == 3) {
-                    const float lz = (float)(k.flow_lbb[2] - z0) - ez,
-                                tz = (float)(k.flow_tfr[2] - z0) - ez;
+                    const float lz = float_from_double(k.flow_lbb[2] - z0) - ez;
+                    const float tz = float_from_double(k.flow_tfr[2] - z0) - ez;
                     inside *= (int)((tz > 0.f && lz < 0.f) || lz * lz <= riSq || tz * tz <= riSq);
                     vpz += !inside * multiplier * fl.z + (float)k.flow_vel[2] * inside;
                 }
                 vpx += !inside * multiplier * fl.x + (float)k.flow_vel[0] * inside;
                 vpy += !inside * multiplier * fl.y + (float)k.flow_vel[1] * inside;
             }
-            if (k.any_wall) {  // addWallVelocity, src/kernels.cu:546-593
+            if (WALLS) {  // addWallVelocity, src/kernels.cu:546-593
+                const float drag = (float)(1.0 - k.wall_drag);
                 float xDrag = 1.f, yDrag = 1.f, velocity = 0.f;
-                if (k.wall[0] && touches_wall_f(f0, rp, (float)(x0 - k.lbb[0]) + ex,
-                                                (float)(x0 - k.tfr[0]) + ex, velocity)) {
+                if (k.wall[0] && touches_wall_f(f0, rp, float_from_double(x0 - k.lbb[0]) + ex,
+                                                float_from_double(x0 - k.tfr[0]) + ex, velocity)) {
                     vpx += velocity;
                     vpy *= drag;
                     vpz *= drag;
                     xDrag = drag;
                 }
                 velocity = 0.f;
-                if (k.wall[1] && touches_wall_f(f0, rp, (float)(y0 - k.lbb[1]) + ey,
-                                                (float)(y0 - k.tfr[1]) + ey, velocity)) {
+                if (k.wall[1] && touches_wall_f(f0, rp, float_from_double(y0 - k.lbb[1]) + ey,
+                                                float_from_double(y0 - k.tfr[1]) + ey, velocity)) {
                     vpx *= drag;
                     vpy += velocity * xDrag;
                     vpz *= drag;
                     yDrag = drag;
                 }
                 velocity = 0.f;
-                if (k.wall[2] && touches_wall_f(f0, rp, (float)(z0 - k.lbb[2]) + ez,
-                                                (float)(z0 - k.tfr[2]) + ez, velocity)) {
+                if (k.wall[2] && touches_wall_f(f0, rp, float_from_double(z0 - k.lbb[2]) + ez,
+                                                float_from_double(z0 - k.tfr[2]) + ez, velocity)) {
                     vpx *= drag;
                     vpy *= drag;
                     vpz += velocity * xDrag * yDrag;
                 }
             }
         }
-        // corrector x + 0.5 ts (v + vp) in FP64 on FP32 rates; the error
+        // corrector x + 0.5 ts (v + vp): FP32 increment, FP64 sum; the error
         // |predicted - corrected| = 0.5 ts |2 v - vo - vp| (src/kernels.cu:487-495)
-        const float sx = vx + vpx, sy = vy + vpy, sz = vz + vpz;
-        const double cx = fma(h64, (double)sx, x0);
-        const double cy = fma(h64, (double)sy, y0);
-        const double cz = DIM == 3 ? fma(h64, (double)sz, z0) : 0.0;
+        const float ix = h * (vx + vpx), iy = h * (vy + vpy), iz = h * (vz + vpz);
+        const double cx = x0 + double_from_float(ix);
+        const double cy = y0 + double_from_float(iy);
+        const double cz = DIM == 3 ? z0 + double_from_float(iz) : 0.0;
         float e = fmaxf(fabsf(fmaf(2.f, vx, -ox) - vpx), fabsf(fmaf(2.f, vy, -oy) - vpy));
         if (DIM == 3) e = fmaxf(e, fabsf(fmaf(2.f, vz, -oz) - vpz));
-        float tx = (float)(cx - S0[i]), ty = (float)(cy - S1[i]);
-        float dist = fmaf(tx, tx, ty * ty);
-        if (DIM == 3) {
-            const float tz = (float)(cz - S2[i]);
-            dist = fmaf(tz, tz, dist);
-        }
-        dist = sqrtf(dist);
+        // expansion since the last search, src/kernels.cu:366-387
+        const float dx = float_from_double(cx - S0[i]), dy = float_from_double(cy - S1[i]);
+        const float dz = DIM == 3 ? float_from_double(cz - S2[i]) : 0.f;
+        float dist = sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
         int del = 0;
-        if (gas) {  // mean-field gas exchange, src/kernels.cu:390-431
+        if (GAS) {  // mean-field gas exchange, src/kernels.cu:390-431
             const float inv = 1.f / rp;
             const float area = DIM == 3 ? (4.f * (float)kPi) * (rp * rp) : (2.f * (float)kPi) * rp;
             float w = (mfa - inv) * (mfb * (area - AO[i])) + vpr;
             w *= DIM == 3 ? kq * (inv * inv) : kq * inv;
             vpr = w;
-            const double cr = fma(h64, (double)(vr + w), r0);
+            const float ir = h * (vr + w);
+            const double cr = r0 + double_from_float(ir);
             e = fmaxf(e, fabsf(fmaf(2.f, vr, -or_) - w));
-            dist += (float)(cr - S3[i]);
-            if (cr > k.min_rad) {
-                vol = fma(DIM == 3 ? cr * cr : cr, cr, vol);
+            dist += float_from_double(cr - S3[i]);
+            if (__double_as_longlong(cr) > minr) {
+                vol = fma(cr * cr, cr, vol);
             } else {
                 del = 1;
                 ndel++;
             }
-            mrad = max_bits(mrad, cr);
+            mrad = max(mrad, __double_as_longlong(cr));
             RN[i] = cr;
             P3[i] = vpr;
             bad |= !finite_bits(cr);
         }
         b.delflag[i] = del;
         mexp = fmaxf(mexp, dist);
-        const double ed = (double)(h * e);
-        merr = max_bits(merr, ed);
-        ERR[i] = fmax(ed, ERR[i]);
+        const double ed = double_from_float(h * e);
+        merr = max(merr, __double_as_longlong(ed));
+        ERR[i] = __longlong_as_double(max(__double_as_longlong(ERR[i]), __double_as_longlong(ed)));
         if (path) {  // src/kernels.cu:437-451
-            float d2 = fmaf(sx, sx, sy * sy);
-            if (DIM == 3) d2 = fmaf(sz, sz, d2);
-            PATHN[i] = PATH[i] + (double)(h * sqrtf(d2));
+            PATHN[i] = PATH[i] + double_from_float(sqrtf(fmaf(iz, iz, fmaf(iy, iy, ix * ix))));
         }
         XN[i] = cx;
         YN[i] = cy;
@@ -381,14 +449,14 @@ __global__ void __launch_bounds__(kBlock) k_correct_mx(Bufs b) {
             P2[i] = vpz;
         }
         bad |= !(finite_bits(cx) && finite_bits(cy) && finite_bits(cz));
-        if (b.dbg_ov) b.dbg_ov[i] = gas ? (double)AO[i] : 0.0;
+        if (b.dbg_ov) b.dbg_ov[i] = GAS ? double_from_float(AO[i]) : 0.0;
         AV[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (gas) AO[i] = 0.f;
-        if (flow) AF[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (GAS) AO[i] = 0.f;
+        if (FLOW) AF[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     const double tErr = block_reduce(__longlong_as_double(merr), OpMax(), smem);
     const double tRad = block_reduce(__longlong_as_double(mrad), OpMax(), smem);
-    const double tExp = block_reduce((double)mexp, OpMax(), smem);
+    const double tExp = block_reduce(double_from_float(mexp), OpMax(), smem);
     const double tVol = block_reduce(vol, OpSum(), smem);
     const int tDel = block_reduce_int(ndel, ismem);
     const int tBad = block_reduce_int(bad, ismem);
@@ -414,14 +482,13 @@ __global__ void __launch_bounds__(kBlock) k_correct_mx(Bufs b) {
 
 // --------------------------------------------------------------- bootstrap
 // phase 0: pred := fixed point of (x, r), vo := 0, path := 0
-// phase 1: euler q += round(acc dt scale), acc := 0
+// phase 1: euler q += fix(acc dt) (src/kernels.cu:959-969), acc := 0
 // phase 2: vo := acc, acc := 0
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_boot_mx(Bufs b, int phase) {
     const Ctrl *c = b.ctrl;
-    const DevConst &k = *b.k;
     const int n = c->n;
-    const double ts = c->dt;
+    const float ts = (float)c->dt;
     const double *X = drow(b, c, RX), *Y = drow(b, c, RY), *Z = drow(b, c, RZ),
                  *R = drow(b, c, RR);
     float *O0 = frow(b, c, RVO0), *O1 = frow(b, c, RVO1), *O2 = frow(b, c, RVO2),
@@ -431,22 +498,21 @@ __global__ void __launch_bounds__(kBlock) k_boot_mx(Bufs b, int phase) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         if (phase == 0) {
             PredMx p;
-            p.q[0] = fixq(k, 0, X[i]);
-            p.q[1] = fixq(k, 1, Y[i]);
-            p.q[2] = DIM == 3 ? fixq(k, 2, Z[i]) : 0ull;
-            p.r = (float)R[i];
+            p.q[0] = fix_from_double(X[i]);
+            p.q[1] = fix_from_double(Y[i]);
+            p.q[2] = DIM == 3 ? fix_from_double(Z[i]) : 0LL;
+            p.r = float_from_double(R[i]);
             p.inv = 1.f / p.r;
             st_pred(b, i, p);
             O0[i] = O1[i] = O2[i] = O3[i] = 0.f;
             PATH[i] = 0.0;
         } else {
             const float4 a = AV[i];
-            if (phase == 1) {  // euler, src/kernels.cu:959-969
+            if (phase == 1) {
                 PredMx p = ld_pred(b, i);
-                p.q[0] += (unsigned long long)__double2ll_rn((double)a.x * ts * k.fx_unit[0]);
-                p.q[1] += (unsigned long long)__double2ll_rn((double)a.y * ts * k.fx_unit[1]);
-                if (DIM == 3)
-                    p.q[2] += (unsigned long long)__double2ll_rn((double)a.z * ts * k.fx_unit[2]);
+                p.q[0] += fix_from_float(a.x * ts);
+                p.q[1] += fix_from_float(a.y * ts);
+                if (DIM == 3) p.q[2] += fix_from_float(a.z * ts);
                 st_pred(b, i, p);
             } else {
                 O0[i] = a.x;
@@ -456,6 +522,18 @@ __global__ void __launch_bounds__(kBlock) k_boot_mx(Bufs b, int phase) {
             AV[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
     }
+}
+
+template <int DIM, bool GAS>
+void launch_correct_mx_t(const Launch &l, const Bufs &b, bool flow, bool walls) {
+    if (flow && walls)
+        k_correct_mx<DIM, GAS, true, true><<<l.grid, kBlock, 0, l.stream>>>(b);
+    else if (flow)
+        k_correct_mx<DIM, GAS, true, false><<<l.grid, kBlock, 0, l.stream>>>(b);
+    else if (walls)
+        k_correct_mx<DIM, GAS, false, true><<<l.grid, kBlock, 0, l.stream>>>(b);
+    else
+        k_correct_mx<DIM, GAS, false, false><<<l.grid, kBlock, 0, l.stream>>>(b);
 }
 
 }  // namespace
@@ -486,11 +564,19 @@ void launch_pairs_mx(const Launch &l, const Bufs &b, int dim, int mode) {
     *l.launches += 1;
 }
 
-void launch_correct_mx(const Launch &l, const Bufs &b, int dim) {
-    if (dim == 3)
-        k_correct_mx<3><<<l.grid, kBlock, 0, l.stream>>>(b);
-    else
-        k_correct_mx<2><<<l.grid, kBlock, 0, l.stream>>>(b);
+void launch_correct_mx(const Launch &l, const Bufs &b, int dim, int mode, bool walls) {
+    const bool gas = mode & 1, flow = mode & 2;
+    if (dim == 3) {
+        if (gas)
+            launch_correct_mx_t<3, true>(l, b, flow, walls);
+        else
+            launch_correct_mx_t<3, false>(l, b, flow, walls);
+    } else {
+        if (gas)
+            launch_correct_mx_t<2, true>(l, b, flow, walls);
+        else
+            launch_correct_mx_t<2, false>(l, b, flow, walls);
+    }
     *l.launches += 1;
 }
 
