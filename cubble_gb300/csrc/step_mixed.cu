@@ -422,7 +422,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_correct_mx(Bufs b) {
             e = fmaxf(e, fabsf(fmaf(2.f, vr, -or_) - w));
             dist += float_from_double(cr - S3[i]);
             if (__double_as_longlong(cr) > minr) {
-                vol = fma(cr * cr, cr, vol);
+                vol = fma(DIM == 3 ? cr * cr : cr, cr, vol);  // sum of r^D
             } else {
                 del = 1;
                 ndel++;
