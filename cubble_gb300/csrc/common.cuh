@@ -70,6 +70,8 @@ struct DevConst {
     // those units.
     long long lq[3], hq[3];
     int mixed;
+    float f0_f;  // f0/mu0 as FP32
+    float kq_f;  // K / (4 pi) in 3D, K / (2 pi) in 2D, as FP32
     float pre_margin;  // FP32 pair-search prefilter margin (length units)
     float half_iv32[3];
     float iv32[3];
@@ -100,6 +102,7 @@ struct Ctrl {
     int np_found;        // pairs found by the last search (may exceed capacity)
     int no_accept;       // cb_attempt: decide dt but do not accept
     double misc_result;  // energy / volume results
+    double mfa, mfb;     // mean-field factors of the attempt (src/kernels.cu:399-404)
     unsigned int done[DC_COUNT];
 };
 
@@ -187,6 +190,35 @@ __device__ __forceinline__ int block_reduce_int(int v, int *smem) {
     return r;
 }
 
+// Block sum of FP32 values: FP32 inside each warp (no FP64 instruction per
+// thread), FP64 across the warps. Result valid in thread 0.
+__device__ __forceinline__ double block_sum_f(float v, double *smem) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if (lane == 0) smem[warp] = (double)v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) r += smem[w];
+    return r;
+}
+
+// Block maximum of 64-bit patterns (doubles >= 0 order like their bits).
+__device__ __forceinline__ long long block_max_bits(long long v, long long *smem) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_down_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if (lane == 0) smem[warp] = v;
+    __syncthreads();
+    long long r = 0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) r = max(r, smem[w]);
+    return r;
+}
+
 // "Last block" pattern: every block publishes its partials, fences, and the
 // block that finishes last does the final (deterministic, in-order)
 // reduction. No block ever waits on another, so nothing can hang.
@@ -206,13 +238,16 @@ __device__ __forceinline__ bool last_block(unsigned int *counter) {
 // Sum / max of this kernel's partials in block order (last block only).
 __device__ __forceinline__ double fold_partials(const double *p, int nblocks, bool is_max,
                                                 double *smem) {
-    double v = 0.0;  // identity of both (all maxima here are of values >= 0)
-    // each thread folds a strided subset in order, then a fixed tree
-    for (int k = threadIdx.x; k < nblocks; k += blockDim.x) {
-        const double t = __ldcg(p + k);
-        v = is_max ? fmax(v, t) : v + t;
+    if (is_max) {  // maxima of values >= 0: integer max of the bit patterns
+        long long m = 0;
+        for (int k = threadIdx.x; k < nblocks; k += blockDim.x)
+            m = max(m, __double_as_longlong(__ldcg(p + k)));
+        return __longlong_as_double(block_max_bits(m, reinterpret_cast<long long *>(smem)));
     }
-    return is_max ? block_reduce(v, OpMax(), smem) : block_reduce(v, OpSum(), smem);
+    double v = 0.0;
+    // each thread folds a strided subset in order, then a fixed tree
+    for (int k = threadIdx.x; k < nblocks; k += blockDim.x) v += __ldcg(p + k);
+    return block_reduce(v, OpSum(), smem);
 }
 
 // ---------------------------------------------------------- FP64 helpers
@@ -385,11 +420,24 @@ __device__ void finish_attempt(Ctrl *c, const DevConst &k, double fErr, double f
 
 // ------------------------------------------------------ kernel launchers
 struct Launch {
-    int grid;         // blocks of every grid-stride kernel (multiple of #SMs)
+    int grid;         // upper bound of the blocks of a grid-stride kernel
+    int sms;          // streaming multiprocessors of the device
     int scan_grid;    // blocks of the scan kernels
     cudaStream_t stream;
     long long *launches;  // host-side launch counter
 };
+
+// One wave of resident blocks of `kernel` (a multiple of the SM count),
+// bounded by l.grid (the size of the per-block partial arrays).
+template <typename K>
+inline int wave_grid(K kernel, const Launch &l) {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kBlock, 0) != cudaSuccess ||
+        nb < 1)
+        nb = 1;
+    const int g = l.sms * nb;
+    return g < l.grid ? g : l.grid;
+}
 
 // step.cu
 void launch_predict(const Launch &l, const Bufs &b, int dim);

@@ -145,6 +145,9 @@ void fill_const(cb_context *c) {
         k.iv32[a] = (float)k.iv[a];
     }
     k.mixed = f.precision == CB_PRECISION_MIXED ? 1 : 0;
+    k.f0_f = (float)k.f0;
+    k.kq_f = (float)(k.dim == 3 ? k.K / (4.0 * 3.1415926535897932384626433832795) :
+                                  k.K / (2.0 * 3.1415926535897932384626433832795));
     for (int a = 0; a < 3; a++) {
         k.lq[a] = (long long)std::llround(k.iv[a] * 1099511627776.0);  // 2^40
         k.hq[a] = k.lq[a] / 2;
@@ -374,6 +377,7 @@ int cb_create(const cb_config *cfg, cb_context **out) {
     fill_const(c);
     const size_t cap = (size_t)c->hk.cap, pcap = (size_t)c->hk.pcap, ccap = (size_t)c->hk.ccap;
     c->launch.grid = std::max(1, c->sms) * 8;
+    c->launch.sms = std::max(1, c->sms);
     c->launch.scan_grid = std::min(1024, std::max(1, c->sms) * 4);
     c->launch.stream = c->stream;
     c->launch.launches = &c->launches;

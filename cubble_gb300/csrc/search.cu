@@ -79,7 +79,8 @@ __global__ void __launch_bounds__(kBlock) k_wrap(Bufs b) {
         b.cellCount[q] = 0;
         b.cellFill[q] = 0;
     }
-    const double t = block_reduce(mr, OpMax(), smem);
+    const double t = __longlong_as_double(
+        block_max_bits(__double_as_longlong(mr), reinterpret_cast<long long *>(smem)));
     if (threadIdx.x == 0) b.part[7 * gridDim.x + blockIdx.x] = t;
     if (last_block(&c->done[DC_WRAP])) {
         const double f = fold_partials(b.part + 7 * gridDim.x, gridDim.x, true, smem);

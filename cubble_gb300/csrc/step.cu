@@ -186,9 +186,13 @@ __global__ void __launch_bounds__(kBlock) k_pairs(Bufs b) {
         const double fAo = fold_partials(b.part + 2 * gridDim.x, gridDim.x, false, smem);
         const double fAor = fold_partials(b.part + 3 * gridDim.x, gridDim.x, false, smem);
         if (threadIdx.x == 0) {
-            b.ctrl->sumAo = 2.0 * fAo;  // each pair adds 2 A_overlap, :267
-            b.ctrl->sumAor = fAor;
-            b.ctrl->done[DC_PAIRS] = 0;
+            Ctrl *cc = b.ctrl;
+            cc->sumAo = 2.0 * fAo;  // each pair adds 2 A_overlap, :267
+            cc->sumAor = fAor;
+            // mean-field factors for every bubble, src/kernels.cu:399-404
+            cc->mfa = (cc->sumAr - cc->sumAor) / (cc->sumA - cc->sumAo);
+            cc->mfb = k.kappa * k.ain * (double)cc->n / cc->sumA;
+            cc->done[DC_PAIRS] = 0;
         }
     }
 }
@@ -234,10 +238,8 @@ __global__ void __launch_bounds__(kBlock) k_correct(Bufs b) {
     const int *NN = irow(b, c, INN);
     // mean-field factors, src/kernels.cu:399-408 (uniform over bubbles);
     // area = 4 pi r^2 (3D) / 2 pi r (2D), so K / area = kq / r^2 (/ r)
-    const double sA = c->sumA, sAr = c->sumAr, sAo = c->sumAo, sAor = c->sumAor;
-    const double mfa = (sAr - sAor) / (sA - sAo);
-    const double mfb = k.kappa * k.ain * (double)n / sA;
-    const double kq = DIM == 3 ? k.K / (4.0 * kPi) : k.K / (2.0 * kPi);
+    const double mfa = c->mfa, mfb = c->mfb;
+    const double kq = DIM == 3 ? k.K * (0.25 / kPi) : k.K * (0.5 / kPi);
     const double drag = 1.0 - k.wall_drag;
     long long merr = 0, mrad = 0, mexp = 0;
     double vol = 0.0;
@@ -369,9 +371,10 @@ __global__ void __launch_bounds__(kBlock) k_correct(Bufs b) {
         reinterpret_cast<double4_32a *>(acc)[0] = zero;
         if (gas || flow) reinterpret_cast<double4_32a *>(acc)[1] = zero;
     }
-    const double tErr = block_reduce(__longlong_as_double(merr), OpMax(), smem);
-    const double tRad = block_reduce(__longlong_as_double(mrad), OpMax(), smem);
-    const double tExp = block_reduce(__longlong_as_double(mexp), OpMax(), smem);
+    long long *lsm = reinterpret_cast<long long *>(smem);
+    const double tErr = __longlong_as_double(block_max_bits(merr, lsm));
+    const double tRad = __longlong_as_double(block_max_bits(mrad, lsm));
+    const double tExp = __longlong_as_double(block_max_bits(mexp, lsm));
     const double tVol = block_reduce(vol, OpSum(), smem);
     const int tDel = block_reduce_int(ndel, ismem);
     const int tBad = block_reduce_int(bad, ismem);
@@ -516,16 +519,17 @@ __global__ void __launch_bounds__(kBlock) k_volume(Bufs b) {
 
 void launch_predict(const Launch &l, const Bufs &b, int dim) {
     if (dim == 3)
-        k_predict<3><<<l.grid, kBlock, 0, l.stream>>>(b);
+        k_predict<3><<<wave_grid(k_predict<3>, l), kBlock, 0, l.stream>>>(b);
     else
-        k_predict<2><<<l.grid, kBlock, 0, l.stream>>>(b);
+        k_predict<2><<<wave_grid(k_predict<2>, l), kBlock, 0, l.stream>>>(b);
     *l.launches += 1;
 }
 
 // mode bits: 1 = gas exchange, 2 = flow. mode 0 is the bootstrap form.
 void launch_pairs(const Launch &l, const Bufs &b, int dim, int mode) {
     const bool gas = mode & 1, flow = mode & 2;
-#define CB_PAIRS(D, G, F) k_pairs<D, G, F><<<l.grid, kBlock, 0, l.stream>>>(b)
+#define CB_PAIRS(D, G, F) \
+    k_pairs<D, G, F><<<wave_grid(k_pairs<D, G, F>, l), kBlock, 0, l.stream>>>(b)
     if (dim == 3) {
         if (gas && flow) CB_PAIRS(3, true, true);
         else if (gas) CB_PAIRS(3, true, false);
@@ -543,9 +547,9 @@ void launch_pairs(const Launch &l, const Bufs &b, int dim, int mode) {
 
 void launch_correct(const Launch &l, const Bufs &b, int dim) {
     if (dim == 3)
-        k_correct<3><<<l.grid, kBlock, 0, l.stream>>>(b);
+        k_correct<3><<<wave_grid(k_correct<3>, l), kBlock, 0, l.stream>>>(b);
     else
-        k_correct<2><<<l.grid, kBlock, 0, l.stream>>>(b);
+        k_correct<2><<<wave_grid(k_correct<2>, l), kBlock, 0, l.stream>>>(b);
     *l.launches += 1;
 }
 

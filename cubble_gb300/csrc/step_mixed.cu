@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(kBlock) k_predict_mx(Bufs b) {
     __shared__ double smem[32];
     const Ctrl *c = b.ctrl;
     const int n = c->n;
-    const float h = (float)(0.5 * c->dt);
+    const float h = float_from_double(0.5 * c->dt);
     const int gas = c->use_gas;
     const double *X = drow(b, c, RX), *Y = drow(b, c, RY), *Z = drow(b, c, RZ),
                  *R = drow(b, c, RR);
@@ -182,8 +182,8 @@ __global__ void __launch_bounds__(kBlock) k_predict_mx(Bufs b) {
             sAr += apr;
         }
     }
-    const double tA = block_reduce(double_from_float(sA), OpSum(), smem);
-    const double tAr = block_reduce(double_from_float(sAr), OpSum(), smem);
+    const double tA = block_sum_f(sA, smem);
+    const double tAr = block_sum_f(sAr, smem);
     if (threadIdx.x == 0) {
         b.part[0 * gridDim.x + blockIdx.x] = tA;
         b.part[1 * gridDim.x + blockIdx.x] = tAr;
@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(kBlock) k_pairs_mx(Bufs b) {
     float4 *AV = acc_v(b);
     float *AO = acc_ov(b, cap);
     float4 *AF = acc_fl(b, cap);
-    const float f0 = (float)k.f0;
+    const float f0 = k.f0_f;
     const bool px = !k.wall[0], py = !k.wall[1], pz = DIM == 3 && !k.wall[2];
     const long long hx = k.hq[0], hy = k.hq[1], hz = k.hq[2];
     const long long lx = k.lq[0], ly = k.lq[1], lz = k.lq[2];
@@ -265,8 +265,8 @@ __global__ void __launch_bounds__(kBlock) k_pairs_mx(Bufs b) {
                 red_add4(AF + i, V0[j], V1[j], DIM == 3 ? V2[j] : 0.f, 0.f);
         }
     }
-    const double tAo = block_reduce(double_from_float(sAo), OpSum(), smem);
-    const double tAor = block_reduce(double_from_float(sAor), OpSum(), smem);
+    const double tAo = block_sum_f(sAo, smem);
+    const double tAor = block_sum_f(sAor, smem);
     if (threadIdx.x == 0) {
         b.part[2 * gridDim.x + blockIdx.x] = tAo;
         b.part[3 * gridDim.x + blockIdx.x] = tAor;
@@ -275,9 +275,13 @@ __global__ void __launch_bounds__(kBlock) k_pairs_mx(Bufs b) {
         const double fAo = fold_partials(b.part + 2 * gridDim.x, gridDim.x, false, smem);
         const double fAor = fold_partials(b.part + 3 * gridDim.x, gridDim.x, false, smem);
         if (threadIdx.x == 0) {
-            b.ctrl->sumAo = 2.0 * fAo;
-            b.ctrl->sumAor = fAor;
-            b.ctrl->done[DC_PAIRS] = 0;
+            Ctrl *cc = b.ctrl;
+            cc->sumAo = 2.0 * fAo;
+            cc->sumAor = fAor;
+            // mean-field factors for every bubble, src/kernels.cu:399-404
+            cc->mfa = (cc->sumAr - cc->sumAor) / (cc->sumA - cc->sumAo);
+            cc->mfb = k.kappa * k.ain * (double)cc->n / cc->sumA;
+            cc->done[DC_PAIRS] = 0;
         }
     }
 }
@@ -304,7 +308,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_correct_mx(Bufs b) {
     const DevConst &k = *b.k;
     const int n = c->n;
     const int cap = k.cap;
-    const float h = (float)(0.5 * c->dt);
+    const float h = float_from_double(0.5 * c->dt);
     const int path = c->inc_path;
     const double *X = drow(b, c, RX), *Y = drow(b, c, RY), *Z = drow(b, c, RZ),
                  *R = drow(b, c, RR);
@@ -323,11 +327,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_correct_mx(Bufs b) {
     float4 *AV = acc_v(b);
     float *AO = acc_ov(b, cap);
     float4 *AF = acc_fl(b, cap);
-    // mean-field factors, src/kernels.cu:399-408, from the FP64 sums
-    const double sA = c->sumA, sAr = c->sumAr, sAo = c->sumAo, sAor = c->sumAor;
-    const float mfa = (float)((sAr - sAor) / (sA - sAo));
-    const float mfb = (float)(k.kappa * k.ain * (double)n / sA);
-    const float kq = (float)(DIM == 3 ? k.K / (4.0 * kPi) : k.K / (2.0 * kPi));
+    // mean-field factors, src/kernels.cu:399-408 (computed once per attempt)
+    const float mfa = float_from_double(c->mfa), mfb = float_from_double(c->mfb);
+    const float kq = k.kq_f;
     const long long minr = __double_as_longlong(k.min_rad);
     long long merr = 0, mrad = 0;
     float mexp = 0.f;
@@ -350,7 +352,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_correct_mx(Bufs b) {
             // predicted coordinates as x0 + e (e the FP32 AB2 increment)
             const float ex = h * fmaf(3.f, vx, -ox), ey = h * fmaf(3.f, vy, -oy),
                         ez = h * fmaf(3.f, vz, -oz);
-            const float f0 = (float)k.f0;
+            const float f0 = k.f0_f;
             if (FLOW) {  // addFlowVelocity, src/kernels.cu:497-544
                 const float4 fl = AF[i];
                 float multiplier = (float)irow(b, c, INN)[i];
@@ -454,9 +456,11 @@ __global__ void __launch_bounds__(kBlock, 2) k_correct_mx(Bufs b) {
         if (GAS) AO[i] = 0.f;
         if (FLOW) AF[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    const double tErr = block_reduce(__longlong_as_double(merr), OpMax(), smem);
-    const double tRad = block_reduce(__longlong_as_double(mrad), OpMax(), smem);
-    const double tExp = block_reduce(double_from_float(mexp), OpMax(), smem);
+    long long *lsm = reinterpret_cast<long long *>(smem);
+    const double tErr = __longlong_as_double(block_max_bits(merr, lsm));
+    const double tRad = __longlong_as_double(block_max_bits(mrad, lsm));
+    const double tExp = __longlong_as_double(
+        block_max_bits(__double_as_longlong(double_from_float(mexp)), lsm));
     const double tVol = block_reduce(vol, OpSum(), smem);
     const int tDel = block_reduce_int(ndel, ismem);
     const int tBad = block_reduce_int(bad, ismem);
@@ -527,28 +531,29 @@ __global__ void __launch_bounds__(kBlock) k_boot_mx(Bufs b, int phase) {
 template <int DIM, bool GAS>
 void launch_correct_mx_t(const Launch &l, const Bufs &b, bool flow, bool walls) {
     if (flow && walls)
-        k_correct_mx<DIM, GAS, true, true><<<l.grid, kBlock, 0, l.stream>>>(b);
+        k_correct_mx<DIM, GAS, true, true><<<wave_grid(k_correct_mx<DIM, GAS, true, true>, l), kBlock, 0, l.stream>>>(b);
     else if (flow)
-        k_correct_mx<DIM, GAS, true, false><<<l.grid, kBlock, 0, l.stream>>>(b);
+        k_correct_mx<DIM, GAS, true, false><<<wave_grid(k_correct_mx<DIM, GAS, true, false>, l), kBlock, 0, l.stream>>>(b);
     else if (walls)
-        k_correct_mx<DIM, GAS, false, true><<<l.grid, kBlock, 0, l.stream>>>(b);
+        k_correct_mx<DIM, GAS, false, true><<<wave_grid(k_correct_mx<DIM, GAS, false, true>, l), kBlock, 0, l.stream>>>(b);
     else
-        k_correct_mx<DIM, GAS, false, false><<<l.grid, kBlock, 0, l.stream>>>(b);
+        k_correct_mx<DIM, GAS, false, false><<<wave_grid(k_correct_mx<DIM, GAS, false, false>, l), kBlock, 0, l.stream>>>(b);
 }
 
 }  // namespace
 
 void launch_predict_mx(const Launch &l, const Bufs &b, int dim) {
     if (dim == 3)
-        k_predict_mx<3><<<l.grid, kBlock, 0, l.stream>>>(b);
+        k_predict_mx<3><<<wave_grid(k_predict_mx<3>, l), kBlock, 0, l.stream>>>(b);
     else
-        k_predict_mx<2><<<l.grid, kBlock, 0, l.stream>>>(b);
+        k_predict_mx<2><<<wave_grid(k_predict_mx<2>, l), kBlock, 0, l.stream>>>(b);
     *l.launches += 1;
 }
 
 void launch_pairs_mx(const Launch &l, const Bufs &b, int dim, int mode) {
     const bool gas = mode & 1, flow = mode & 2;
-#define CB_PAIRS(D, G, F) k_pairs_mx<D, G, F><<<l.grid, kBlock, 0, l.stream>>>(b)
+#define CB_PAIRS(D, G, F) \
+    k_pairs_mx<D, G, F><<<wave_grid(k_pairs_mx<D, G, F>, l), kBlock, 0, l.stream>>>(b)
     if (dim == 3) {
         if (gas && flow) CB_PAIRS(3, true, true);
         else if (gas) CB_PAIRS(3, true, false);
