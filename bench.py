@@ -285,7 +285,10 @@ def measure_form(args, world, rank, precision, clocks_on=True):
     step_gbs = ab["step"] * n_now / (sum(kms) * 1e-3) / 1e9
     gas, flow = int(cfg.use_gas_exchange), int(cfg.use_flow)
     sfx = "_mx" if precision else ""
-    kname = {"predict": "k_predict%s<%d>" % (sfx, dim), "correct": "k_correct%s<%d>" % (sfx, dim),
+    walls = int(any(cfg.wall[:dim]))
+    kcorr = ("k_correct_mx<%d, %d, %d, %d>" % (dim, gas, flow, walls) if precision
+             else "k_correct<%d>" % dim)
+    kname = {"predict": "k_predict%s<%d>" % (sfx, dim), "correct": kcorr,
              "pairs": "k_pairs%s<%d, %d, %d>" % (sfx, dim, gas, flow)}[names[top]]
     tr = profiled_traffic(kname)
     roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": hbm,

@@ -103,6 +103,11 @@ struct Ctrl {
     int no_accept;       // cb_attempt: decide dt but do not accept
     double misc_result;  // energy / volume results
     double mfa, mfb;     // mean-field factors of the attempt (src/kernels.cu:399-404)
+    // Order-independent attempt reductions of the one-bubble-per-thread
+    // correct kernel: maxima as 64-bit patterns of doubles >= 0 and counts;
+    // zero between attempts (the kernel's last block reads and clears them).
+    long long amax_err, amax_rad, amax_exp;
+    int acnt_del, acnt_bad;
     unsigned int done[DC_COUNT];
 };
 
@@ -423,6 +428,7 @@ struct Launch {
     int grid;         // upper bound of the blocks of a grid-stride kernel
     int sms;          // streaming multiprocessors of the device
     int scan_grid;    // blocks of the scan kernels
+    int cover;        // blocks of a one-bubble-per-thread kernel over capacity
     cudaStream_t stream;
     long long *launches;  // host-side launch counter
 };

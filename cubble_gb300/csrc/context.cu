@@ -379,9 +379,10 @@ int cb_create(const cb_config *cfg, cb_context **out) {
     c->launch.grid = std::max(1, c->sms) * 8;
     c->launch.sms = std::max(1, c->sms);
     c->launch.scan_grid = std::min(1024, std::max(1, c->sms) * 4);
+    c->launch.cover = (int)((cap + kBlock - 1) / kBlock);
     c->launch.stream = c->stream;
     c->launch.launches = &c->launches;
-    const int G = c->launch.grid;
+    const int G = std::max(c->launch.grid, c->launch.cover);
     if (cudaMallocHost(&c->hctrl, sizeof(Ctrl)) != cudaSuccess)
         return bail(fail(CB_ERR_CUDA, "cudaMallocHost"));
     std::memset(c->hctrl, 0, sizeof(Ctrl));

@@ -109,7 +109,8 @@ __device__ __forceinline__ long long wrap_fix(long long d, long long half, long 
 
 // Accumulator layout of the mixed form inside `acc` (64 bytes per bubble):
 // float4 velocity sums (vx, vy, vz, vr) at [0, 16 cap), float overlap at
-// [16 cap, 20 cap), float4 flow sums at [32 cap, 48 cap) bytes.
+// [16 cap, 20 cap), float4 flow sums at [32 cap, 48 cap) bytes. In 2D the
+// velocity float4 is (vx, vy, overlap, vr) and the overlap row is unused.
 __device__ __forceinline__ float4 *acc_v(const Bufs &b) { return reinterpret_cast<float4 *>(b.acc); }
 __device__ __forceinline__ float *acc_ov(const Bufs &b, int cap) {
     return reinterpret_cast<float *>(b.acc) + 4 * (size_t)cap;
@@ -200,6 +201,14 @@ __global__ void __launch_bounds__(kBlock) k_predict_mx(Bufs b) {
 }
 
 // ------------------------------------------------------------------ pairs
+// The search emits the pairs grouped by i in ascending order, so consecutive
+// pairs mostly share their first bubble. Each thread takes a run of kRun
+// consecutive pairs (one 16-byte load of the i's and one of the j's), loads
+// the prediction of i once per distinct i, keeps i's sums in registers and
+// adds them with one vector reduction per distinct i; the j side adds per
+// pair. In 2D the overlap sum rides in the third lane of the velocity float4.
+constexpr int kRun = 4;
+
 template <int DIM, bool GAS, bool FLOW>
 __global__ void __launch_bounds__(kBlock) k_pairs_mx(Bufs b) {
     __shared__ double smem[32];
@@ -218,52 +227,109 @@ __global__ void __launch_bounds__(kBlock) k_pairs_mx(Bufs b) {
     const long long hx = k.hq[0], hy = k.hq[1], hz = k.hq[2];
     const long long lx = k.lq[0], ly = k.lq[1], lz = k.lq[2];
     float sAo = 0.f, sAor = 0.f;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
-        const int i = PI[p], j = PJ[p];
-        if (FLOW)  // src/kernels.cu:191-207 (added for every pair)
-            red_add4(AF + j, V0[i], V1[i], DIM == 3 ? V2[i] : 0.f, 0.f);
-        const PredMx a = ld_pred(b, i), q = ld_pred(b, j);
-        long long ex = a.q[0] - q.q[0], ey = a.q[1] - q.q[1], ez = 0;
-        if (px) ex = wrap_fix(ex, hx, lx);
-        if (py) ey = wrap_fix(ey, hy, ly);
-        if (DIM == 3) {
-            ez = a.q[2] - q.q[2];
-            if (pz) ez = wrap_fix(ez, hz, lz);
-        }
-        const float dx = len_from_fix(ex), dy = len_from_fix(ey);
-        const float dz = DIM == 3 ? len_from_fix(ez) : 0.f;
-        const float r1 = a.r, r2 = q.r;
-        float m = dx * dx;
-        m = fmaf(dy, dy, m);
-        if (DIM == 3) m = fmaf(dz, dz, m);
-        const float radii = r1 + r2;
-        if (radii * radii >= m) {
-            // velocity f0 d (1/|d| - 1/(r1 + r2)), src/kernels.cu:218-233
-            const float rs = rsqrtf(m);
-            const float s = f0 * (rs - __fdividef(1.f, radii));
-            const float fx = dx * s, fy = dy * s, fz = dz * s;
-            float g = 0.f;
-            if (GAS) {  // pairwise gas exchange, src/kernels.cu:236-280
-                const float r1sq = r1 * r1, r2sq = r2 * r2;
-                float oa;
-                if (m < r1sq || m < r2sq) {
-                    oa = DIM == 3 ? fminf(r1sq, r2sq) * (float)kPi : 2.f * fminf(r1, r2);
-                } else {
-                    const float t = 0.5f * (r2sq - r1sq + m);
-                    oa = fabsf(r2sq - (t * t) * (rs * rs));
-                    oa = DIM == 3 ? oa * (float)kPi : 2.f * sqrtf(oa);
-                }
-                g = oa * (q.inv - a.inv);
-                atomicAdd(AO + i, oa);
-                atomicAdd(AO + j, oa);
-                sAo += oa;
-                sAor = fmaf(oa, a.inv + q.inv, sAor);
+    const int nrun = (np + kRun - 1) / kRun;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < nrun; g += gridDim.x * blockDim.x) {
+        const int p0 = g * kRun;
+        int I[kRun], J[kRun];
+        if (p0 + kRun <= np) {
+            const int4 u = *reinterpret_cast<const int4 *>(PI + p0);
+            const int4 v = *reinterpret_cast<const int4 *>(PJ + p0);
+            I[0] = u.x; I[1] = u.y; I[2] = u.z; I[3] = u.w;
+            J[0] = v.x; J[1] = v.y; J[2] = v.z; J[3] = v.w;
+        } else {
+#pragma unroll
+            for (int t = 0; t < kRun; t++) {
+                I[t] = p0 + t < np ? PI[p0 + t] : -1;
+                J[t] = p0 + t < np ? PJ[p0 + t] : 0;
             }
-            red_add4(AV + i, fx, fy, fz, g);
-            red_add4(AV + j, -fx, -fy, -fz, -g);
-            if (FLOW)  // src/kernels.cu:298-307 (overlapping pairs only)
-                red_add4(AF + i, V0[j], V1[j], DIM == 3 ? V2[j] : 0.f, 0.f);
         }
+        int cur = -1;
+        PredMx a;
+        float ax = 0.f, ay = 0.f, az = 0.f, ag = 0.f, ao = 0.f;
+        float fx_i = 0.f, fy_i = 0.f, fz_i = 0.f, vxi = 0.f, vyi = 0.f, vzi = 0.f;
+        bool hit = false;
+        auto flush = [&]() {
+            if (DIM == 3) {
+                red_add4(AV + cur, ax, ay, az, ag);
+                if (GAS) atomicAdd(AO + cur, ao);
+            } else {
+                red_add4(AV + cur, ax, ay, ao, ag);
+            }
+            if (FLOW) red_add4(AF + cur, fx_i, fy_i, fz_i, 0.f);
+        };
+#pragma unroll
+        for (int t = 0; t < kRun; t++) {
+            const int i = I[t], j = J[t];
+            if (i < 0) break;
+            if (i != cur) {
+                if (hit) flush();
+                cur = i;
+                a = ld_pred(b, i);
+                ax = ay = az = ag = ao = 0.f;
+                fx_i = fy_i = fz_i = 0.f;
+                hit = false;
+                if (FLOW) {
+                    vxi = V0[i];
+                    vyi = V1[i];
+                    vzi = DIM == 3 ? V2[i] : 0.f;
+                }
+            }
+            if (FLOW)  // src/kernels.cu:191-207 (added for every pair)
+                red_add4(AF + j, vxi, vyi, vzi, 0.f);
+            const PredMx q = ld_pred(b, j);
+            long long ex = a.q[0] - q.q[0], ey = a.q[1] - q.q[1], ez = 0;
+            if (px) ex = wrap_fix(ex, hx, lx);
+            if (py) ey = wrap_fix(ey, hy, ly);
+            if (DIM == 3) {
+                ez = a.q[2] - q.q[2];
+                if (pz) ez = wrap_fix(ez, hz, lz);
+            }
+            const float dx = len_from_fix(ex), dy = len_from_fix(ey);
+            const float dz = DIM == 3 ? len_from_fix(ez) : 0.f;
+            const float r1 = a.r, r2 = q.r;
+            float m = dx * dx;
+            m = fmaf(dy, dy, m);
+            if (DIM == 3) m = fmaf(dz, dz, m);
+            const float radii = r1 + r2;
+            if (radii * radii >= m) {
+                // velocity f0 d (1/|d| - 1/(r1 + r2)), src/kernels.cu:218-233
+                const float rs = rsqrtf(m);
+                const float s = f0 * (rs - __fdividef(1.f, radii));
+                const float fx = dx * s, fy = dy * s, fz = dz * s;
+                float gf = 0.f, oa = 0.f;
+                if (GAS) {  // pairwise gas exchange, src/kernels.cu:236-280
+                    const float r1sq = r1 * r1, r2sq = r2 * r2;
+                    if (m < r1sq || m < r2sq) {
+                        oa = DIM == 3 ? fminf(r1sq, r2sq) * (float)kPi : 2.f * fminf(r1, r2);
+                    } else {
+                        const float tt = 0.5f * (r2sq - r1sq + m);
+                        oa = fabsf(r2sq - (tt * tt) * (rs * rs));
+                        oa = DIM == 3 ? oa * (float)kPi : 2.f * sqrtf(oa);
+                    }
+                    gf = oa * (q.inv - a.inv);
+                    sAo += oa;
+                    sAor = fmaf(oa, a.inv + q.inv, sAor);
+                }
+                ax += fx;
+                ay += fy;
+                az += fz;
+                ag += gf;
+                ao += oa;
+                hit = true;
+                if (DIM == 3) {
+                    red_add4(AV + j, -fx, -fy, -fz, -gf);
+                    if (GAS) atomicAdd(AO + j, oa);
+                } else {
+                    red_add4(AV + j, -fx, -fy, oa, -gf);
+                }
+                if (FLOW) {  // src/kernels.cu:298-307 (overlapping pairs only)
+                    fx_i += V0[j];
+                    fy_i += V1[j];
+                    if (DIM == 3) fz_i += V2[j];
+                }
+            }
+        }
+        if (hit) flush();
     }
     const double tAo = block_sum_f(sAo, smem);
     const double tAor = block_sum_f(sAor, smem);
@@ -300,30 +366,74 @@ __device__ __forceinline__ bool touches_wall_f(float f0, float rad, float d1, fl
     return false;
 }
 
+// Row pointers of the correct kernel come from a per-block table in shared
+// memory, fetched at each use with a volatile load: a grid-stride loop would
+// otherwise keep all ~27 role-resolved 64-bit pointers in registers across
+// its iterations (119 registers in 3D, two blocks per SM; with the table
+// 64 registers and four blocks per SM).
+__device__ __forceinline__ void *tab_ptr(const unsigned long long *tab, int r) {
+    unsigned long long p;
+    asm volatile("ld.shared.u64 %0, [%1];"
+                 : "=l"(p)
+                 : "r"((unsigned int)__cvta_generic_to_shared(tab + r)));
+    return reinterpret_cast<void *>(p);
+}
+
+// One pass over the block for the correct kernel's five reductions: maxima of
+// error, radius and expansion (64-bit patterns of doubles >= 0), the volume
+// sum (FP64, fixed order for a fixed block size) and the deletion and
+// non-finite counts. Results valid in thread 0.
+struct CorrRed {
+    long long err, rad, exp;
+    double vol;
+    int del, bad;
+};
+
+__device__ __forceinline__ CorrRed block_reduce_corr(CorrRed v, CorrRed *smem) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v.err = max(v.err, __shfl_down_sync(0xffffffffu, v.err, o));
+        v.rad = max(v.rad, __shfl_down_sync(0xffffffffu, v.rad, o));
+        v.exp = max(v.exp, __shfl_down_sync(0xffffffffu, v.exp, o));
+        v.vol += __shfl_down_sync(0xffffffffu, v.vol, o);
+        v.del += __shfl_down_sync(0xffffffffu, v.del, o);
+        v.bad += __shfl_down_sync(0xffffffffu, v.bad, o);
+    }
+    if (lane == 0) smem[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
+            const CorrRed u = smem[w];
+            v.err = max(v.err, u.err);
+            v.rad = max(v.rad, u.rad);
+            v.exp = max(v.exp, u.exp);
+            v.vol += u.vol;
+            v.del += u.del;
+            v.bad += u.bad;
+        }
+    return v;
+}
+
+// Grid-stride over the bubbles (one wave of blocks). The maxima and counts go
+// to the control block with integer atomics (order-independent); only the
+// volume sum keeps per-block partials for its in-order FP64 fold.
 template <int DIM, bool GAS, bool FLOW, bool WALLS>
-__global__ void __launch_bounds__(kBlock, 2) k_correct_mx(Bufs b) {
+__global__ void __launch_bounds__(kBlock, 4) k_correct_mx(Bufs b) {
     __shared__ double smem[32];
-    __shared__ int ismem[32];
+    __shared__ CorrRed rsm[kBlock / 32];
+    __shared__ unsigned long long tab[ND_ROLES];
     Ctrl *c = b.ctrl;
     const DevConst &k = *b.k;
     const int n = c->n;
     const int cap = k.cap;
+    if (threadIdx.x < ND_ROLES)
+        tab[threadIdx.x] = reinterpret_cast<unsigned long long>(b.ds[c->drole[threadIdx.x]]);
+    __syncthreads();
+#define CB_D(r) reinterpret_cast<double *>(tab_ptr(tab, r))
+#define CB_F(r) reinterpret_cast<float *>(tab_ptr(tab, r))
     const float h = float_from_double(0.5 * c->dt);
     const int path = c->inc_path;
-    const double *X = drow(b, c, RX), *Y = drow(b, c, RY), *Z = drow(b, c, RZ),
-                 *R = drow(b, c, RR);
-    double *XN = drow(b, c, RXN), *YN = drow(b, c, RYN), *ZN = drow(b, c, RZN),
-           *RN = drow(b, c, RRN);
-    const float *V0 = frow(b, c, RV0), *V1 = frow(b, c, RV1), *V2 = frow(b, c, RV2),
-                *V3 = frow(b, c, RV3);
-    const float *O0 = frow(b, c, RVO0), *O1 = frow(b, c, RVO1), *O2 = frow(b, c, RVO2),
-                *O3 = frow(b, c, RVO3);
-    float *P0 = frow(b, c, RVP0), *P1 = frow(b, c, RVP1), *P2 = frow(b, c, RVP2),
-          *P3 = frow(b, c, RVP3);
-    const double *S0 = drow(b, c, RS0), *S1 = drow(b, c, RS1), *S2 = drow(b, c, RS2),
-                 *S3 = drow(b, c, RS3);
-    const double *PATH = drow(b, c, RPATH);
-    double *PATHN = drow(b, c, RPATHN), *ERR = drow(b, c, RERR);
     float4 *AV = acc_v(b);
     float *AO = acc_ov(b, cap);
     float4 *AF = acc_fl(b, cap);
@@ -337,15 +447,17 @@ __global__ void __launch_bounds__(kBlock, 2) k_correct_mx(Bufs b) {
     int ndel = 0, bad = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 a = AV[i];
-        float vpx = a.x, vpy = a.y, vpz = a.z, vpr = a.w;
-        const float vx = V0[i], vy = V1[i], vz = DIM == 3 ? V2[i] : 0.f;
-        const float ox = O0[i], oy = O1[i], oz = DIM == 3 ? O2[i] : 0.f;
-        const double x0 = X[i], y0 = Y[i], z0 = DIM == 3 ? Z[i] : 0.0, r0 = R[i];
+        float vpx = a.x, vpy = a.y, vpz = DIM == 3 ? a.z : 0.f, vpr = a.w;
+        const float ovl = GAS ? (DIM == 3 ? AO[i] : a.z) : 0.f;  // overlap area sum
+        const float vx = CB_F(RV0)[i], vy = CB_F(RV1)[i], vz = DIM == 3 ? CB_F(RV2)[i] : 0.f;
+        const float ox = CB_F(RVO0)[i], oy = CB_F(RVO1)[i], oz = DIM == 3 ? CB_F(RVO2)[i] : 0.f;
+        const double x0 = CB_D(RX)[i], y0 = CB_D(RY)[i], z0 = DIM == 3 ? CB_D(RZ)[i] : 0.0;
+        const double r0 = CB_D(RR)[i];
         float vr = 0.f, or_ = 0.f;
         float rp = float_from_double(r0);
         if (GAS) {
-            vr = V3[i];
-            or_ = O3[i];
+            vr = CB_F(RV3)[i];
+            or_ = CB_F(RVO3)[i];
             rp = fmaf(h, fmaf(3.f, vr, -or_), rp);  // as k_predict_mx
         }
         if (FLOW || WALLS) {
@@ -409,20 +521,21 @@ __global__ void __launch_bounds__(kBlock, 2) k_correct_mx(Bufs b) {
         float e = fmaxf(fabsf(fmaf(2.f, vx, -ox) - vpx), fabsf(fmaf(2.f, vy, -oy) - vpy));
         if (DIM == 3) e = fmaxf(e, fabsf(fmaf(2.f, vz, -oz) - vpz));
         // expansion since the last search, src/kernels.cu:366-387
-        const float dx = float_from_double(cx - S0[i]), dy = float_from_double(cy - S1[i]);
-        const float dz = DIM == 3 ? float_from_double(cz - S2[i]) : 0.f;
+        const float dx = float_from_double(cx - CB_D(RS0)[i]);
+        const float dy = float_from_double(cy - CB_D(RS1)[i]);
+        const float dz = DIM == 3 ? float_from_double(cz - CB_D(RS2)[i]) : 0.f;
         float dist = sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
         int del = 0;
         if (GAS) {  // mean-field gas exchange, src/kernels.cu:390-431
             const float inv = 1.f / rp;
             const float area = DIM == 3 ? (4.f * (float)kPi) * (rp * rp) : (2.f * (float)kPi) * rp;
-            float w = (mfa - inv) * (mfb * (area - AO[i])) + vpr;
+            float w = (mfa - inv) * (mfb * (area - ovl)) + vpr;
             w *= DIM == 3 ? kq * (inv * inv) : kq * inv;
             vpr = w;
             const float ir = h * (vr + w);
             const double cr = r0 + double_from_float(ir);
             e = fmaxf(e, fabsf(fmaf(2.f, vr, -or_) - w));
-            dist += float_from_double(cr - S3[i]);
+            dist += float_from_double(cr - CB_D(RS3)[i]);
             if (__double_as_longlong(cr) > minr) {
                 vol = fma(DIM == 3 ? cr * cr : cr, cr, vol);  // sum of r^D
             } else {
@@ -430,57 +543,56 @@ __global__ void __launch_bounds__(kBlock, 2) k_correct_mx(Bufs b) {
                 ndel++;
             }
             mrad = max(mrad, __double_as_longlong(cr));
-            RN[i] = cr;
-            P3[i] = vpr;
+            CB_D(RRN)[i] = cr;
+            CB_F(RVP3)[i] = vpr;
             bad |= !finite_bits(cr);
         }
         b.delflag[i] = del;
         mexp = fmaxf(mexp, dist);
         const double ed = double_from_float(h * e);
         merr = max(merr, __double_as_longlong(ed));
+        double *ERR = CB_D(RERR);
         ERR[i] = __longlong_as_double(max(__double_as_longlong(ERR[i]), __double_as_longlong(ed)));
         if (path) {  // src/kernels.cu:437-451
-            PATHN[i] = PATH[i] + double_from_float(sqrtf(fmaf(iz, iz, fmaf(iy, iy, ix * ix))));
+            CB_D(RPATHN)[i] = CB_D(RPATH)[i] +
+                              double_from_float(sqrtf(fmaf(iz, iz, fmaf(iy, iy, ix * ix))));
         }
-        XN[i] = cx;
-        YN[i] = cy;
-        P0[i] = vpx;
-        P1[i] = vpy;
+        CB_D(RXN)[i] = cx;
+        CB_D(RYN)[i] = cy;
+        CB_F(RVP0)[i] = vpx;
+        CB_F(RVP1)[i] = vpy;
         if (DIM == 3) {
-            ZN[i] = cz;
-            P2[i] = vpz;
+            CB_D(RZN)[i] = cz;
+            CB_F(RVP2)[i] = vpz;
         }
         bad |= !(finite_bits(cx) && finite_bits(cy) && finite_bits(cz));
-        if (b.dbg_ov) b.dbg_ov[i] = GAS ? double_from_float(AO[i]) : 0.0;
+        if (b.dbg_ov) b.dbg_ov[i] = double_from_float(ovl);
         AV[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (GAS) AO[i] = 0.f;
+        if (GAS && DIM == 3) AO[i] = 0.f;
         if (FLOW) AF[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    long long *lsm = reinterpret_cast<long long *>(smem);
-    const double tErr = __longlong_as_double(block_max_bits(merr, lsm));
-    const double tRad = __longlong_as_double(block_max_bits(mrad, lsm));
-    const double tExp = __longlong_as_double(
-        block_max_bits(__double_as_longlong(double_from_float(mexp)), lsm));
-    const double tVol = block_reduce(vol, OpSum(), smem);
-    const int tDel = block_reduce_int(ndel, ismem);
-    const int tBad = block_reduce_int(bad, ismem);
-    const int G = gridDim.x;
+#undef CB_D
+#undef CB_F
+    CorrRed v{merr, mrad, __double_as_longlong(double_from_float(mexp)), vol, ndel, bad};
+    v = block_reduce_corr(v, rsm);
     if (threadIdx.x == 0) {
-        b.part[0 * G + blockIdx.x] = tErr;
-        b.part[1 * G + blockIdx.x] = tRad;
-        b.part[2 * G + blockIdx.x] = tExp;
-        b.part[3 * G + blockIdx.x] = tVol;
-        b.part[4 * G + blockIdx.x] = (double)tDel;
-        b.part[5 * G + blockIdx.x] = (double)tBad;
+        atomicMax(&c->amax_err, v.err);
+        atomicMax(&c->amax_rad, v.rad);
+        atomicMax(&c->amax_exp, v.exp);
+        if (v.del) atomicAdd(&c->acnt_del, v.del);
+        if (v.bad) atomicAdd(&c->acnt_bad, v.bad);
+        b.part[blockIdx.x] = v.vol;
     }
     if (!last_block(&c->done[DC_CORRECT])) return;
-    const double fErr = fold_partials(b.part + 0 * G, G, true, smem);
-    const double fRad = fold_partials(b.part + 1 * G, G, true, smem);
-    const double fExp = fold_partials(b.part + 2 * G, G, true, smem);
-    const double fVol = fold_partials(b.part + 3 * G, G, false, smem);
-    const double fDel = fold_partials(b.part + 4 * G, G, false, smem);
-    const double fBad = fold_partials(b.part + 5 * G, G, false, smem);
+    const double fVol = fold_partials(b.part, gridDim.x, false, smem);
     if (threadIdx.x != 0) return;
+    volatile Ctrl *vc = c;
+    const double fErr = __longlong_as_double(vc->amax_err);
+    const double fRad = __longlong_as_double(vc->amax_rad);
+    const double fExp = __longlong_as_double(vc->amax_exp);
+    const double fDel = (double)vc->acnt_del, fBad = (double)vc->acnt_bad;
+    c->amax_err = c->amax_rad = c->amax_exp = 0;
+    c->acnt_del = c->acnt_bad = 0;
     finish_attempt<DIM>(c, k, fErr, fRad, fExp, fVol, fDel, fBad);
 }
 
