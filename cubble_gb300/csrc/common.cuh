@@ -108,6 +108,10 @@ struct Ctrl {
     // zero between attempts (the kernel's last block reads and clears them).
     long long amax_err, amax_rad, amax_exp;
     int acnt_del, acnt_bad;
+    // Batched launches (several foams per launch): which phases this foam
+    // takes part in next (BatchSel bits, set between launches) and the
+    // number of blocks of its virtual grid.
+    int bsel, vgrid;
     unsigned int done[DC_COUNT];
 };
 
@@ -227,13 +231,14 @@ __device__ __forceinline__ long long block_max_bits(long long v, long long *smem
 // "Last block" pattern: every block publishes its partials, fences, and the
 // block that finishes last does the final (deterministic, in-order)
 // reduction. No block ever waits on another, so nothing can hang.
-__device__ __forceinline__ bool last_block(unsigned int *counter) {
+// `total` is the number of blocks that take part (the virtual grid size).
+__device__ __forceinline__ bool last_block(unsigned int *counter, int total) {
     __shared__ bool am_last;
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
         const unsigned int prev = atomicAdd(counter, 1u);
-        am_last = (prev == gridDim.x - 1);
+        am_last = (prev == (unsigned int)total - 1u);
     }
     __syncthreads();
     if (am_last) __threadfence();
@@ -431,7 +436,57 @@ struct Launch {
     int cover;        // blocks of a one-bubble-per-thread kernel over capacity
     cudaStream_t stream;
     long long *launches;  // host-side launch counter
+    // Batched launches: when `batch` is set, every launcher runs its kernel's
+    // batched form over `count` foams (device table of their Bufs) on a
+    // dim3(gmax, count) grid, for the foams whose Ctrl::bsel has `sel`.
+    const struct Bufs *batch = nullptr;
+    int count = 0, gmax = 0, sel = 0;
 };
+
+// Phases of a batched step a foam takes part in (Ctrl::bsel bits).
+enum BatchSel : int { SEL_ATTEMPT = 1, SEL_DELETE = 2, SEL_SEARCH = 4 };
+
+// Batched form of a kernel: blockIdx.y picks the foam; its blocks
+// 0 .. vgrid-1 run the body with (vb, vg) = (blockIdx.x, vgrid) in place of
+// (blockIdx.x, gridDim.x); the other blocks, and every block of a foam that
+// is not selected, return at once. Returns false for those.
+__device__ __forceinline__ bool batch_slot(const Bufs *bb, int sel, Bufs &b, int &vb, int &vg) {
+    const Ctrl *c = bb[blockIdx.y].ctrl;
+    if (!(c->bsel & sel)) return false;
+    vg = c->vgrid;
+    if ((int)blockIdx.x >= vg) return false;
+    vb = blockIdx.x;
+    b = bb[blockIdx.y];
+    return true;
+}
+
+#define CB_ID(...) __VA_ARGS__
+
+// Declares the single-foam kernel NAME(Bufs) and its batched form
+// NAME_batch(const Bufs *, int sel) around the body NAME_body(b, vb, vg).
+// TPL is the parenthesised template header ("(template <int DIM>)" or "()"),
+// ARGS the parenthesised template arguments ("(<DIM>)" or "()").
+#define CB_KERNEL_PAIR(TPL, NAME, ARGS, BOUNDS)                                  \
+    CB_ID TPL __global__ void BOUNDS NAME(Bufs b) {                                \
+        NAME##_body CB_ID ARGS(b, blockIdx.x, gridDim.x);                          \
+    }                                                                              \
+    CB_ID TPL __global__ void BOUNDS NAME##_batch(const Bufs *bb, int sel) {       \
+        Bufs b;                                                                    \
+        int vb, vg;                                                                \
+        if (!batch_slot(bb, sel, b, vb, vg)) return;                               \
+        NAME##_body CB_ID ARGS(b, vb, vg);                                         \
+    }
+
+// Launches NAME<ARGS> in its single or batched form per the Launch `l`.
+#define CB_LAUNCH(l, NAME, ARGS, GRID, b)                                             \
+    do {                                                                             \
+        if ((l).batch)                                                               \
+            NAME##_batch CB_ID ARGS<<<dim3((l).gmax, (l).count), kBlock, 0, (l).stream>>>( \
+                (l).batch, (l).sel);                                                 \
+        else                                                                         \
+            NAME CB_ID ARGS<<<(GRID), kBlock, 0, (l).stream>>>(b);                   \
+        *(l).launches += 1;                                                          \
+    } while (0)
 
 // One wave of resident blocks of `kernel` (a multiple of the SM count),
 // bounded by l.grid (the size of the per-block partial arrays).
@@ -462,7 +517,10 @@ void launch_search(const Launch &l, const Bufs &b, int dim);
 // remove.cu
 void launch_remove(const Launch &l, const Bufs &b, int dim);
 // scan.cu
-void launch_scan(const Launch &l, const Bufs &b, const int *in, int *out, const int *count_ptr,
-                 int count_add, int *total_out);
+// Exclusive scans of the search and the deletion: cellCount -> cellStart
+// (ncell), rowCount -> rowStart (n, total -> np_found), delflag -> iscan (n),
+// keep -> keepScan (np); out[count] = total.
+enum ScanKind : int { SCAN_CELLS = 0, SCAN_ROWS, SCAN_DEL, SCAN_KEEP };
+void launch_scan(const Launch &l, const Bufs &b, int kind);
 
 }  // namespace cbg

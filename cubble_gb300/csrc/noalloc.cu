@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(kBlock) k_na_sum(double *s, int n, double *out
     double *part = s + kMaxBubbles;
     if (threadIdx.x == 0) part[blockIdx.x] = t;
     unsigned int *done = reinterpret_cast<unsigned int *>(s + kMaxBubbles + kBlocks);
-    if (last_block(done)) {
+    if (last_block(done, gridDim.x)) {
         const double f = fold_partials(part, gridDim.x, false, smem);
         if (threadIdx.x == 0) {
             *out = f;

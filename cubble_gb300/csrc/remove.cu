@@ -15,28 +15,30 @@ namespace cbg {
 namespace {
 
 // holes[k] = k-th deleted index below nNew; keep flags of the pairs.
-__global__ void __launch_bounds__(kBlock) k_remove_a(Bufs b) {
+__device__ __forceinline__ void k_remove_a_body(const Bufs &b, const int vb, const int vg) {
     const Ctrl *c = b.ctrl;
     const int n = c->n, D = c->ndel, nNew = n - D, np = c->np;
     const int *PI = b.ps[c->prole[PI0]];
     const int *PJ = b.ps[c->prole[PJ0]];
-    const int stride = gridDim.x * blockDim.x;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nNew; i += stride)
+    const int stride = vg * blockDim.x;
+    for (int i = vb * blockDim.x + threadIdx.x; i < nNew; i += stride)
         if (b.delflag[i]) b.holes[b.iscan[i]] = i;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride)
+    for (int p = vb * blockDim.x + threadIdx.x; p < np; p += stride)
         b.keep[p] = !(b.delflag[PI[p]] | b.delflag[PJ[p]]);
 }
+CB_KERNEL_PAIR((), k_remove_a, (), __launch_bounds__(kBlock))
+
 
 // Survivors at or above nNew move into the holes.
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_remove_b(Bufs b) {
+__device__ __forceinline__ void k_remove_b_body(const Bufs &b, const int vb, const int vg) {
     const Ctrl *c = b.ctrl;
     const int n = c->n, D = c->ndel, nNew = n - D;
     static constexpr int kRoles[] = {RX, RY, RZ, RR, RV0, RV1, RV2, RV3, RVO0, RVO1, RVO2, RVO3,
                                      RS0, RS1, RS2, RS3, RPATH, RERR};
     static constexpr int kIRoles[] = {IWX, IWY, IWZ, IIDX, INN};
-    for (int i = nNew + blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += gridDim.x * blockDim.x) {
+    for (int i = nNew + vb * blockDim.x + threadIdx.x; i < n;
+         i += vg * blockDim.x) {
         if (b.delflag[i]) continue;
         // survivors after i: (n - 1 - i) - (deleted after i)
         const int rank = (n - 1 - i) - (D - b.iscan[i]);
@@ -59,10 +61,12 @@ __global__ void __launch_bounds__(kBlock) k_remove_b(Bufs b) {
         }
     }
 }
+CB_KERNEL_PAIR((template <int DIM>), k_remove_b, (<DIM>), __launch_bounds__(kBlock))
+
 
 // Pair compaction + remap, the volume fix and the bookkeeping.
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_remove_c(Bufs b) {
+__device__ __forceinline__ void k_remove_c_body(const Bufs &b, const int vb, const int vg) {
     Ctrl *c = b.ctrl;
     const DevConst &k = *b.k;
     const int n = c->n, D = c->ndel, nNew = n - D, np = c->np;
@@ -70,8 +74,8 @@ __global__ void __launch_bounds__(kBlock) k_remove_c(Bufs b) {
     const int *PJ = b.ps[c->prole[PJ0]];
     int *QI = b.ps[c->prole[PI1]];
     int *QJ = b.ps[c->prole[PJ1]];
-    const int stride = gridDim.x * blockDim.x;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
+    const int stride = vg * blockDim.x;
+    for (int p = vb * blockDim.x + threadIdx.x; p < np; p += stride) {
         if (!b.keep[p]) continue;
         int e1 = PI[p], e2 = PJ[p];
         if (e1 >= nNew) e1 = b.moveDst[e1];
@@ -85,9 +89,9 @@ __global__ void __launch_bounds__(kBlock) k_remove_c(Bufs b) {
     volMul = DIM == 3 ? rcbrt(volMul) : rsqrt(volMul);
     volMul *= k.vol_mul_const;
     double *R = drow(b, c, RR);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nNew; i += stride)
+    for (int i = vb * blockDim.x + threadIdx.x; i < nNew; i += stride)
         R[i] = R[i] * volMul;
-    if (last_block(&c->done[DC_REMOVE]) && threadIdx.x == 0) {
+    if (last_block(&c->done[DC_REMOVE], vg) && threadIdx.x == 0) {
         swap_role(c->prole, PI0, PI1);
         swap_role(c->prole, PJ0, PJ1);
         c->np = b.keepScan[np];
@@ -99,25 +103,24 @@ __global__ void __launch_bounds__(kBlock) k_remove_c(Bufs b) {
         c->done[DC_REMOVE] = 0;
     }
 }
+CB_KERNEL_PAIR((template <int DIM>), k_remove_c, (<DIM>), __launch_bounds__(kBlock))
+
 
 }  // namespace
 
 void launch_remove(const Launch &l, const Bufs &b, int dim) {
     const int G = l.grid;
-    Ctrl *c = b.ctrl;
-    launch_scan(l, b, b.delflag, b.iscan, &c->n, 0, nullptr);
-    k_remove_a<<<G, kBlock, 0, l.stream>>>(b);
+    launch_scan(l, b, SCAN_DEL);
+    CB_LAUNCH(l, k_remove_a, (), G, b);
     if (dim == 3)
-        k_remove_b<3><<<G, kBlock, 0, l.stream>>>(b);
+        CB_LAUNCH(l, k_remove_b, (<3>), G, b);
     else
-        k_remove_b<2><<<G, kBlock, 0, l.stream>>>(b);
-    *l.launches += 2;
-    launch_scan(l, b, b.keep, b.keepScan, &c->np, 0, nullptr);
+        CB_LAUNCH(l, k_remove_b, (<2>), G, b);
+    launch_scan(l, b, SCAN_KEEP);
     if (dim == 3)
-        k_remove_c<3><<<G, kBlock, 0, l.stream>>>(b);
+        CB_LAUNCH(l, k_remove_c, (<3>), G, b);
     else
-        k_remove_c<2><<<G, kBlock, 0, l.stream>>>(b);
-    *l.launches += 1;
+        CB_LAUNCH(l, k_remove_c, (<2>), G, b);
 }
 
 }  // namespace cbg

@@ -13,22 +13,37 @@
 namespace cbg {
 namespace {
 
-__device__ __forceinline__ int read_count(const int *count_ptr, int add) {
-    return *count_ptr + add;
+// What a scan reads and writes, per use in the search and the deletion.
+struct ScanIO {
+    const int *in;
+    int *out;
+    int count;
+    int *total_out;
+};
+
+__device__ __forceinline__ ScanIO scan_io(const Bufs &b, int kind) {
+    Ctrl *c = b.ctrl;
+    switch (kind) {
+        case SCAN_CELLS: return {b.cellCount, b.cellStart, c->ncell, nullptr};
+        case SCAN_ROWS: return {b.rowCount, b.rowStart, c->n, &c->np_found};
+        case SCAN_DEL: return {b.delflag, b.iscan, c->n, nullptr};
+        default: return {b.keep, b.keepScan, c->np, nullptr};
+    }
 }
 
-__global__ void __launch_bounds__(kBlock) k_scan_sums(const int *in, const int *count_ptr,
-                                                      int add, int *blocksums) {
+template <int KIND>
+__device__ __forceinline__ void k_scan_sums_body(const Bufs &b, const int vb, const int vg) {
     __shared__ int smem[32];
-    const int count = read_count(count_ptr, add);
-    const int chunk = (count + gridDim.x - 1) / gridDim.x;
-    const int s = blockIdx.x * chunk;
-    const int e = min(s + chunk, count);
+    const ScanIO io = scan_io(b, KIND);
+    const int chunk = (io.count + vg - 1) / vg;
+    const int s = vb * chunk;
+    const int e = min(s + chunk, io.count);
     int v = 0;
-    for (int i = s + threadIdx.x; i < e; i += blockDim.x) v += in[i];
+    for (int i = s + threadIdx.x; i < e; i += blockDim.x) v += io.in[i];
     v = block_reduce_int(v, smem);
-    if (threadIdx.x == 0) blocksums[blockIdx.x] = v;
+    if (threadIdx.x == 0) b.blocksums[vb] = v;
 }
+CB_KERNEL_PAIR((template <int KIND>), k_scan_sums, (<KIND>), __launch_bounds__(kBlock))
 
 // Block-wide exclusive scan; returns the exclusive prefix of `v` and writes
 // the block total into *total.
@@ -59,7 +74,7 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *smem, int *total
     return warp_off + x - v;
 }
 
-__global__ void __launch_bounds__(1024) k_scan_top(int *blocksums, int nblocks) {
+__device__ __forceinline__ void k_scan_top_body(int *blocksums, int nblocks) {
     __shared__ int smem[32];
     __shared__ int carry_s;
     if (threadIdx.x == 0) carry_s = 0;
@@ -78,44 +93,66 @@ __global__ void __launch_bounds__(1024) k_scan_top(int *blocksums, int nblocks) 
     if (threadIdx.x == 0) blocksums[nblocks] = carry_s;
 }
 
-__global__ void __launch_bounds__(kBlock) k_scan_apply(const int *in, int *out, const int *count_ptr,
-                                                       int add, const int *blocksums,
-                                                       int *total_out) {
+__global__ void __launch_bounds__(1024) k_scan_top(int *blocksums, int nblocks) {
+    k_scan_top_body(blocksums, nblocks);
+}
+
+// Batched form: one block per selected foam, over its virtual grid's sums.
+__global__ void __launch_bounds__(1024) k_scan_top_batch(const Bufs *bb, int sel) {
+    const Bufs &b = bb[blockIdx.y];
+    if (!(b.ctrl->bsel & sel)) return;
+    k_scan_top_body(b.blocksums, b.ctrl->vgrid);
+}
+
+template <int KIND>
+__device__ __forceinline__ void k_scan_apply_body(const Bufs &b, const int vb, const int vg) {
     __shared__ int smem[32];
     __shared__ int carry_s;
-    const int count = read_count(count_ptr, add);
-    const int chunk = (count + gridDim.x - 1) / gridDim.x;
-    const int s = blockIdx.x * chunk;
-    const int e = min(s + chunk, count);
-    if (threadIdx.x == 0) carry_s = blocksums[blockIdx.x];
+    const ScanIO io = scan_io(b, KIND);
+    const int chunk = (io.count + vg - 1) / vg;
+    const int s = vb * chunk;
+    const int e = min(s + chunk, io.count);
+    if (threadIdx.x == 0) carry_s = b.blocksums[vb];
     __syncthreads();
     for (int base = s; base < e; base += blockDim.x) {
         const int i = base + threadIdx.x;
-        const int v = i < e ? in[i] : 0;
+        const int v = i < e ? io.in[i] : 0;
         int tot;
         const int ex = block_exclusive_scan(v, smem, &tot);
         const int carry = carry_s;
-        if (i < e) out[i] = carry + ex;
+        if (i < e) io.out[i] = carry + ex;
         __syncthreads();
         if (threadIdx.x == 0) carry_s = carry + tot;
         __syncthreads();
     }
-    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
-        const int total = blocksums[gridDim.x];
-        out[count] = total;
-        if (total_out) *total_out = total;
+    if (vb == vg - 1 && threadIdx.x == 0) {
+        const int total = b.blocksums[vg];
+        io.out[io.count] = total;
+        if (io.total_out) *io.total_out = total;
     }
+}
+CB_KERNEL_PAIR((template <int KIND>), k_scan_apply, (<KIND>), __launch_bounds__(kBlock))
+
+template <int KIND>
+void launch_scan_t(const Launch &l, const Bufs &b) {
+    CB_LAUNCH(l, k_scan_sums, (<KIND>), l.scan_grid, b);
+    if (l.batch)
+        k_scan_top_batch<<<dim3(1, l.count), 1024, 0, l.stream>>>(l.batch, l.sel);
+    else
+        k_scan_top<<<1, 1024, 0, l.stream>>>(b.blocksums, l.scan_grid);
+    *l.launches += 1;
+    CB_LAUNCH(l, k_scan_apply, (<KIND>), l.scan_grid, b);
 }
 
 }  // namespace
 
-void launch_scan(const Launch &l, const Bufs &b, const int *in, int *out, const int *count_ptr,
-                 int count_add, int *total_out) {
-    k_scan_sums<<<l.scan_grid, kBlock, 0, l.stream>>>(in, count_ptr, count_add, b.blocksums);
-    k_scan_top<<<1, 1024, 0, l.stream>>>(b.blocksums, l.scan_grid);
-    k_scan_apply<<<l.scan_grid, kBlock, 0, l.stream>>>(in, out, count_ptr, count_add, b.blocksums,
-                                                      total_out);
-    *l.launches += 3;
+void launch_scan(const Launch &l, const Bufs &b, int kind) {
+    switch (kind) {
+        case SCAN_CELLS: launch_scan_t<SCAN_CELLS>(l, b); break;
+        case SCAN_ROWS: launch_scan_t<SCAN_ROWS>(l, b); break;
+        case SCAN_DEL: launch_scan_t<SCAN_DEL>(l, b); break;
+        default: launch_scan_t<SCAN_KEEP>(l, b); break;
+    }
 }
 
 }  // namespace cbg

@@ -52,7 +52,7 @@ __device__ __forceinline__ int cell_coord(double x, double lbb, double iv, int c
 }
 
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_wrap(Bufs b) {
+__device__ __forceinline__ void k_wrap_body(const Bufs &b, const int vb, const int vg) {
     __shared__ double smem[32];
     Ctrl *c = b.ctrl;
     const DevConst &k = *b.k;
@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(kBlock) k_wrap(Bufs b) {
     int *WR[3] = {irow(b, c, IWX), irow(b, c, IWY), irow(b, c, IWZ)};
     const double *R = drow(b, c, RR);
     double mr = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int i = vb * blockDim.x + threadIdx.x; i < n; i += vg * blockDim.x) {
 #pragma unroll
         for (int a = 0; a < DIM; a++) {
             if (k.wall[a]) continue;
@@ -75,15 +75,15 @@ __global__ void __launch_bounds__(kBlock) k_wrap(Bufs b) {
         }
         mr = fmax(mr, R[i]);
     }
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q <= k.ccap; q += gridDim.x * blockDim.x) {
+    for (int q = vb * blockDim.x + threadIdx.x; q <= k.ccap; q += vg * blockDim.x) {
         b.cellCount[q] = 0;
         b.cellFill[q] = 0;
     }
     const double t = __longlong_as_double(
         block_max_bits(__double_as_longlong(mr), reinterpret_cast<long long *>(smem)));
-    if (threadIdx.x == 0) b.part[7 * gridDim.x + blockIdx.x] = t;
-    if (last_block(&c->done[DC_WRAP])) {
-        const double f = fold_partials(b.part + 7 * gridDim.x, gridDim.x, true, smem);
+    if (threadIdx.x == 0) b.part[7 * vg + vb] = t;
+    if (last_block(&c->done[DC_WRAP], vg)) {
+        const double f = fold_partials(b.part + 7 * vg, vg, true, smem);
         if (threadIdx.x == 0) {
             int cd[3];
             cell_grid(k, f, cd);
@@ -96,15 +96,17 @@ __global__ void __launch_bounds__(kBlock) k_wrap(Bufs b) {
         }
     }
 }
+CB_KERNEL_PAIR((template <int DIM>), k_wrap, (<DIM>), __launch_bounds__(kBlock))
+
 
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_cell_count(Bufs b) {
+__device__ __forceinline__ void k_cell_count_body(const Bufs &b, const int vb, const int vg) {
     const Ctrl *c = b.ctrl;
     const DevConst &k = *b.k;
     const int n = c->n;
     const int cd0 = c->cell_dims[0], cd1 = c->cell_dims[1], cd2 = c->cell_dims[2];
     const double *X = drow(b, c, RX), *Y = drow(b, c, RY), *Z = drow(b, c, RZ);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int i = vb * blockDim.x + threadIdx.x; i < n; i += vg * blockDim.x) {
         const int kx = cell_coord(X[i], k.lbb[0], k.iv[0], cd0);
         const int ky = cell_coord(Y[i], k.lbb[1], k.iv[1], cd1);
         const int kz = DIM == 3 ? cell_coord(Z[i], k.lbb[2], k.iv[2], cd2) : 0;
@@ -113,22 +115,26 @@ __global__ void __launch_bounds__(kBlock) k_cell_count(Bufs b) {
         atomicAdd(b.cellCount + ci, 1);
     }
 }
+CB_KERNEL_PAIR((template <int DIM>), k_cell_count, (<DIM>), __launch_bounds__(kBlock))
 
-__global__ void __launch_bounds__(kBlock) k_cell_fill(Bufs b) {
+
+__device__ __forceinline__ void k_cell_fill_body(const Bufs &b, const int vb, const int vg) {
     const int n = b.ctrl->n;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int i = vb * blockDim.x + threadIdx.x; i < n; i += vg * blockDim.x) {
         const int ci = b.cellOf[i];
         b.perm[b.cellStart[ci] + atomicAdd(b.cellFill + ci, 1)] = i;
     }
 }
+CB_KERNEL_PAIR((), k_cell_fill, (), __launch_bounds__(kBlock))
+
 
 // One warp per cell: rank each member by its previous position (values are
 // distinct), giving the stable counting-sort order.
-__global__ void __launch_bounds__(kBlock) k_cell_order(Bufs b) {
+__device__ __forceinline__ void k_cell_order_body(const Bufs &b, const int vb, const int vg) {
     const int ncell = b.ctrl->ncell;
     const int lane = threadIdx.x & 31;
-    const int warps = gridDim.x * (blockDim.x >> 5);
-    for (int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); q < ncell; q += warps) {
+    const int warps = vg * (blockDim.x >> 5);
+    for (int q = vb * (blockDim.x >> 5) + (threadIdx.x >> 5); q < ncell; q += warps) {
         const int s = b.cellStart[q], e = b.cellStart[q + 1], m = e - s;
         for (int t0 = 0; t0 < m; t0 += 32) {
             const int t = t0 + lane;
@@ -142,14 +148,16 @@ __global__ void __launch_bounds__(kBlock) k_cell_order(Bufs b) {
         }
     }
 }
+CB_KERNEL_PAIR((), k_cell_order, (), __launch_bounds__(kBlock))
+
 
 // Gathers a rate row (FP64, or FP32 in the mixed form) into another slot.
 __device__ __forceinline__ void gather_rate(const Bufs &b, const Ctrl *c, int from_role,
-                                            int to_role, const int *src, int n) {
+                                            int to_role, const int *src, int n, int vb, int vg) {
     const bool f32 = b.k->mixed;
     const double *from = drow(b, c, from_role);
     double *to = drow(b, c, to_role);
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    for (int q = vb * blockDim.x + threadIdx.x; q < n; q += vg * blockDim.x) {
         if (f32)
             reinterpret_cast<float *>(to)[q] = reinterpret_cast<const float *>(from)[src[q]];
         else
@@ -160,7 +168,7 @@ __device__ __forceinline__ void gather_rate(const Bufs &b, const Ctrl *c, int fr
 // Gather pass A: positions (+ saved), velocities, path, error, wrap counts
 // and indices into their spare slots, then swap the roles.
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_permute_a(Bufs b) {
+__device__ __forceinline__ void k_permute_a_body(const Bufs &b, const int vb, const int vg) {
     Ctrl *c = b.ctrl;
     const int n = c->n;
     const int *src = b.permSorted;
@@ -172,7 +180,7 @@ __global__ void __launch_bounds__(kBlock) k_permute_a(Bufs b) {
         double *sv = drow(b, c, RS0 + a);
         pos[a] = to;
         if (DIM == 2 && a == 2) continue;
-        for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        for (int q = vb * blockDim.x + threadIdx.x; q < n; q += vg * blockDim.x) {
             const double v = from[src[q]];
             to[q] = v;
             sv[q] = v;
@@ -180,12 +188,12 @@ __global__ void __launch_bounds__(kBlock) k_permute_a(Bufs b) {
     }
     for (int a = 0; a < 4; a++) {
         if (DIM == 2 && a == 2) continue;
-        gather_rate(b, c, RV0 + a, RVP0 + a, src, n);
+        gather_rate(b, c, RV0 + a, RVP0 + a, src, n, vb, vg);
     }
     {
         const double *f1 = drow(b, c, RPATH), *f2 = drow(b, c, RERR);
         double *t1 = drow(b, c, RPATHN), *t2 = drow(b, c, RERR2);
-        for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        for (int q = vb * blockDim.x + threadIdx.x; q < n; q += vg * blockDim.x) {
             const int s = src[q];
             t1[q] = f1[s];
             t2[q] = f2[s];
@@ -194,7 +202,7 @@ __global__ void __launch_bounds__(kBlock) k_permute_a(Bufs b) {
     {
         const int *f[4] = {irow(b, c, IWX), irow(b, c, IWY), irow(b, c, IWZ), irow(b, c, IIDX)};
         int *t[4] = {irow(b, c, IWX2), irow(b, c, IWY2), irow(b, c, IWZ2), irow(b, c, IIDX2)};
-        for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        for (int q = vb * blockDim.x + threadIdx.x; q < n; q += vg * blockDim.x) {
             const int s = src[q];
             t[0][q] = f[0][s];
             t[1][q] = f[1][s];
@@ -202,11 +210,11 @@ __global__ void __launch_bounds__(kBlock) k_permute_a(Bufs b) {
             t[3][q] = f[3][s];
         }
     }
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    for (int q = vb * blockDim.x + threadIdx.x; q < n; q += vg * blockDim.x) {
         b.pos32[q] = make_float4((float)pos[0][q], (float)pos[1][q],
                                  DIM == 3 ? (float)pos[2][q] : 0.0f, (float)pos[3][q]);
     }
-    if (last_block(&c->done[DC_PERMUTE]) && threadIdx.x == 0) {
+    if (last_block(&c->done[DC_PERMUTE], vg) && threadIdx.x == 0) {
         int *r = c->drole;
         for (int a = 0; a < 4; a++) {
             if (DIM == 2 && a == 2) continue;
@@ -223,18 +231,20 @@ __global__ void __launch_bounds__(kBlock) k_permute_a(Bufs b) {
         c->done[DC_PERMUTE] = 0;
     }
 }
+CB_KERNEL_PAIR((template <int DIM>), k_permute_a, (<DIM>), __launch_bounds__(kBlock))
+
 
 // Gather pass B: previous velocities into the slot the old velocities left.
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_permute_b(Bufs b) {
+__device__ __forceinline__ void k_permute_b_body(const Bufs &b, const int vb, const int vg) {
     Ctrl *c = b.ctrl;
     const int n = c->n;
     const int *src = b.permSorted;
     for (int a = 0; a < 4; a++) {
         if (DIM == 2 && a == 2) continue;
-        gather_rate(b, c, RVO0 + a, RVP0 + a, src, n);
+        gather_rate(b, c, RVO0 + a, RVP0 + a, src, n, vb, vg);
     }
-    if (last_block(&c->done[DC_PERMUTE]) && threadIdx.x == 0) {
+    if (last_block(&c->done[DC_PERMUTE], vg) && threadIdx.x == 0) {
         for (int a = 0; a < 4; a++) {
             if (DIM == 2 && a == 2) continue;
             swap_role(c->drole, RVO0 + a, RVP0 + a);
@@ -242,6 +252,8 @@ __global__ void __launch_bounds__(kBlock) k_permute_b(Bufs b) {
         c->done[DC_PERMUTE] = 0;
     }
 }
+CB_KERNEL_PAIR((template <int DIM>), k_permute_b, (<DIM>), __launch_bounds__(kBlock))
+
 
 // Neighbour cell `k` (0..26, offsets dx,dy,dz in -1..1) of `cell`, or
 // INT_MAX when it is below `cell` in linear order, outside a wall, on an
@@ -298,7 +310,7 @@ constexpr int kWarpsPerBlock = kBlock / 32;
 // runs, so the pair set equals the FP64 one bit for bit.
 // WRITE = false counts rows, WRITE = true writes them at rowStart.
 template <int DIM, bool WRITE>
-__global__ void __launch_bounds__(kBlock) k_pair_cells(Bufs b) {
+__device__ __forceinline__ void k_pair_cells_body(const Bufs &b, const int vb, const int vg) {
     __shared__ float4 stage[kWarpsPerBlock][32];
     Ctrl *c = b.ctrl;
     const DevConst &k = *b.k;
@@ -313,8 +325,8 @@ __global__ void __launch_bounds__(kBlock) k_pair_cells(Bufs b) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const float skin32 = (float)k.skin, band = k.pre_margin;
     const bool per[3] = {!k.wall[0], !k.wall[1], !k.wall[2]};
-    const int warps = gridDim.x * kWarpsPerBlock;
-    for (int cell = blockIdx.x * kWarpsPerBlock + w; cell < ncell; cell += warps) {
+    const int warps = vg * kWarpsPerBlock;
+    for (int cell = vb * kWarpsPerBlock + w; cell < ncell; cell += warps) {
         const int s0 = b.cellStart[cell], e0 = b.cellStart[cell + 1];
         if (s0 == e0) continue;
         const int nbr = warp_sort(lane < 27 ? neighbor_cell<DIM>(k, cd, cell, lane) : 0x7fffffff);
@@ -382,7 +394,7 @@ __global__ void __launch_bounds__(kBlock) k_pair_cells(Bufs b) {
             }
         }
     }
-    if (WRITE && last_block(&c->done[DC_MISC]) && threadIdx.x == 0) {
+    if (WRITE && last_block(&c->done[DC_MISC], vg) && threadIdx.x == 0) {
         const int found = c->np_found;
         if (found > pcap) {
             c->status = CB_ERR_CAPACITY;
@@ -394,51 +406,49 @@ __global__ void __launch_bounds__(kBlock) k_pair_cells(Bufs b) {
         c->done[DC_MISC] = 0;
     }
 }
+CB_KERNEL_PAIR((template <int DIM, bool WRITE>), k_pair_cells, (<DIM, WRITE>), __launch_bounds__(kBlock))
 
-__global__ void __launch_bounds__(kBlock) k_degree(Bufs b) {
+
+__device__ __forceinline__ void k_degree_body(const Bufs &b, const int vb, const int vg) {
     const Ctrl *c = b.ctrl;
     const int np = c->np;
     const int *PJ = b.ps[c->prole[PJ0]];
     int *NN = b.is[c->irole[INN]];
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x)
+    for (int p = vb * blockDim.x + threadIdx.x; p < np; p += vg * blockDim.x)
         atomicAdd(NN + PJ[p], 1);
 }
+CB_KERNEL_PAIR((), k_degree, (), __launch_bounds__(kBlock))
+
 
 }  // namespace
 
 void launch_search(const Launch &l, const Bufs &b, int dim) {
     const int G = l.grid;
-    cudaStream_t s = l.stream;
-    Ctrl *c = b.ctrl;
     if (dim == 3) {
-        k_wrap<3><<<G, kBlock, 0, s>>>(b);
-        k_cell_count<3><<<G, kBlock, 0, s>>>(b);
+        CB_LAUNCH(l, k_wrap, (<3>), G, b);
+        CB_LAUNCH(l, k_cell_count, (<3>), G, b);
     } else {
-        k_wrap<2><<<G, kBlock, 0, s>>>(b);
-        k_cell_count<2><<<G, kBlock, 0, s>>>(b);
+        CB_LAUNCH(l, k_wrap, (<2>), G, b);
+        CB_LAUNCH(l, k_cell_count, (<2>), G, b);
     }
-    *l.launches += 2;
-    launch_scan(l, b, b.cellCount, b.cellStart, &c->ncell, 0, nullptr);
-    k_cell_fill<<<G, kBlock, 0, s>>>(b);
-    k_cell_order<<<G, kBlock, 0, s>>>(b);
-    *l.launches += 2;
+    launch_scan(l, b, SCAN_CELLS);
+    CB_LAUNCH(l, k_cell_fill, (), G, b);
+    CB_LAUNCH(l, k_cell_order, (), G, b);
     if (dim == 3) {
-        k_permute_a<3><<<G, kBlock, 0, s>>>(b);
-        k_permute_b<3><<<G, kBlock, 0, s>>>(b);
-        k_pair_cells<3, false><<<G, kBlock, 0, s>>>(b);
+        CB_LAUNCH(l, k_permute_a, (<3>), G, b);
+        CB_LAUNCH(l, k_permute_b, (<3>), G, b);
+        CB_LAUNCH(l, k_pair_cells, (<3, false>), G, b);
     } else {
-        k_permute_a<2><<<G, kBlock, 0, s>>>(b);
-        k_permute_b<2><<<G, kBlock, 0, s>>>(b);
-        k_pair_cells<2, false><<<G, kBlock, 0, s>>>(b);
+        CB_LAUNCH(l, k_permute_a, (<2>), G, b);
+        CB_LAUNCH(l, k_permute_b, (<2>), G, b);
+        CB_LAUNCH(l, k_pair_cells, (<2, false>), G, b);
     }
-    *l.launches += 3;
-    launch_scan(l, b, b.rowCount, b.rowStart, &c->n, 0, &c->np_found);
+    launch_scan(l, b, SCAN_ROWS);
     if (dim == 3)
-        k_pair_cells<3, true><<<G, kBlock, 0, s>>>(b);
+        CB_LAUNCH(l, k_pair_cells, (<3, true>), G, b);
     else
-        k_pair_cells<2, true><<<G, kBlock, 0, s>>>(b);
-    k_degree<<<G, kBlock, 0, s>>>(b);
-    *l.launches += 2;
+        CB_LAUNCH(l, k_pair_cells, (<2, true>), G, b);
+    CB_LAUNCH(l, k_degree, (), G, b);
 }
 
 }  // namespace cbg

@@ -25,7 +25,7 @@ __device__ __forceinline__ double4_32a ld4(const double *p, int i) {
 
 // ---------------------------------------------------------------- predict
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_predict(Bufs b) {
+__device__ __forceinline__ void k_predict_body(const Bufs &b, const int vb, const int vg) {
     __shared__ double smem[32];
     const Ctrl *c = b.ctrl;
     const int n = c->n;
@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(kBlock) k_predict(Bufs b) {
     const double *O0 = drow(b, c, RVO0), *O1 = drow(b, c, RVO1), *O2 = drow(b, c, RVO2),
                  *O3 = drow(b, c, RVO3);
     double sA = 0.0, sAr = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int i = vb * blockDim.x + threadIdx.x; i < n; i += vg * blockDim.x) {
         // p + 0.5 ts (3 v - vo), src/kernels.cu:48-50
         const double xp = fma(h, fma(3.0, V0[i], -O0[i]), X[i]);
         const double yp = fma(h, fma(3.0, V1[i], -O1[i]), Y[i]);
@@ -68,12 +68,12 @@ __global__ void __launch_bounds__(kBlock) k_predict(Bufs b) {
     const double tA = block_reduce(sA, OpSum(), smem);
     const double tAr = block_reduce(sAr, OpSum(), smem);
     if (threadIdx.x == 0) {
-        b.part[0 * gridDim.x + blockIdx.x] = tA;
-        b.part[1 * gridDim.x + blockIdx.x] = tAr;
+        b.part[0 * vg + vb] = tA;
+        b.part[1 * vg + vb] = tAr;
     }
-    if (last_block(&b.ctrl->done[DC_PREDICT])) {
-        const double fA = fold_partials(b.part + 0 * gridDim.x, gridDim.x, false, smem);
-        const double fAr = fold_partials(b.part + 1 * gridDim.x, gridDim.x, false, smem);
+    if (last_block(&b.ctrl->done[DC_PREDICT], vg)) {
+        const double fA = fold_partials(b.part + 0 * vg, vg, false, smem);
+        const double fAr = fold_partials(b.part + 1 * vg, vg, false, smem);
         if (threadIdx.x == 0) {
             b.ctrl->sumA = fA;
             b.ctrl->sumAr = fAr;
@@ -81,6 +81,8 @@ __global__ void __launch_bounds__(kBlock) k_predict(Bufs b) {
         }
     }
 }
+CB_KERNEL_PAIR((template <int DIM>), k_predict, (<DIM>), __launch_bounds__(kBlock))
+
 
 // ------------------------------------------------------------------ pairs
 // One lane per pair; contributions to both members go through FP64 atomics
@@ -89,7 +91,7 @@ __global__ void __launch_bounds__(kBlock) k_predict(Bufs b) {
 // rcp_hn, the division by m of the overlap formula as a product with
 // (1/sqrt(m))^2.
 template <int DIM, bool GAS, bool FLOW>
-__global__ void __launch_bounds__(kBlock) k_pairs(Bufs b) {
+__device__ __forceinline__ void k_pairs_body(const Bufs &b, const int vb, const int vg) {
     __shared__ double smem[32];
     const Ctrl *c = b.ctrl;
     const DevConst &k = *b.k;
@@ -102,7 +104,7 @@ __global__ void __launch_bounds__(kBlock) k_pairs(Bufs b) {
     const double hx = k.half_iv[0], hy = k.half_iv[1], hz = k.half_iv[2];
     const double Lx = k.iv[0], Ly = k.iv[1], Lz = k.iv[2];
     double sAo = 0.0, sAor = 0.0;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+    for (int p = vb * blockDim.x + threadIdx.x; p < np; p += vg * blockDim.x) {
         const int i = PI[p], j = PJ[p];
         double *ai = b.acc + (size_t)i * kAcc;
         double *aj = b.acc + (size_t)j * kAcc;
@@ -179,12 +181,12 @@ __global__ void __launch_bounds__(kBlock) k_pairs(Bufs b) {
     const double tAo = block_reduce(sAo, OpSum(), smem);
     const double tAor = block_reduce(sAor, OpSum(), smem);
     if (threadIdx.x == 0) {
-        b.part[2 * gridDim.x + blockIdx.x] = tAo;
-        b.part[3 * gridDim.x + blockIdx.x] = tAor;
+        b.part[2 * vg + vb] = tAo;
+        b.part[3 * vg + vb] = tAor;
     }
-    if (last_block(&b.ctrl->done[DC_PAIRS])) {
-        const double fAo = fold_partials(b.part + 2 * gridDim.x, gridDim.x, false, smem);
-        const double fAor = fold_partials(b.part + 3 * gridDim.x, gridDim.x, false, smem);
+    if (last_block(&b.ctrl->done[DC_PAIRS], vg)) {
+        const double fAo = fold_partials(b.part + 2 * vg, vg, false, smem);
+        const double fAor = fold_partials(b.part + 3 * vg, vg, false, smem);
         if (threadIdx.x == 0) {
             Ctrl *cc = b.ctrl;
             cc->sumAo = 2.0 * fAo;  // each pair adds 2 A_overlap, :267
@@ -196,6 +198,8 @@ __global__ void __launch_bounds__(kBlock) k_pairs(Bufs b) {
         }
     }
 }
+CB_KERNEL_PAIR((template <int DIM, bool GAS, bool FLOW>), k_pairs, (<DIM, GAS, FLOW>), __launch_bounds__(kBlock))
+
 
 // ---------------------------------------------------------------- correct
 // touchesWall, src/kernels.cu:553-566
@@ -214,7 +218,7 @@ __device__ __forceinline__ bool touches_wall(double f0, double rad, double x, do
 }
 
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_correct(Bufs b) {
+__device__ __forceinline__ void k_correct_body(const Bufs &b, const int vb, const int vg) {
     __shared__ double smem[32];
     __shared__ int ismem[32];
     Ctrl *c = b.ctrl;
@@ -244,7 +248,7 @@ __global__ void __launch_bounds__(kBlock) k_correct(Bufs b) {
     long long merr = 0, mrad = 0, mexp = 0;
     double vol = 0.0;
     int ndel = 0, bad = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int i = vb * blockDim.x + threadIdx.x; i < n; i += vg * blockDim.x) {
         double *acc = b.acc + (size_t)i * kAcc;
         const double4_32a a0 = reinterpret_cast<const double4_32a *>(acc)[0];
         double4_32a a1;
@@ -378,16 +382,16 @@ __global__ void __launch_bounds__(kBlock) k_correct(Bufs b) {
     const double tVol = block_reduce(vol, OpSum(), smem);
     const int tDel = block_reduce_int(ndel, ismem);
     const int tBad = block_reduce_int(bad, ismem);
-    const int G = gridDim.x;
+    const int G = vg;
     if (threadIdx.x == 0) {
-        b.part[0 * G + blockIdx.x] = tErr;
-        b.part[1 * G + blockIdx.x] = tRad;
-        b.part[2 * G + blockIdx.x] = tExp;
-        b.part[3 * G + blockIdx.x] = tVol;
-        b.part[4 * G + blockIdx.x] = (double)tDel;
-        b.part[5 * G + blockIdx.x] = (double)tBad;
+        b.part[0 * G + vb] = tErr;
+        b.part[1 * G + vb] = tRad;
+        b.part[2 * G + vb] = tExp;
+        b.part[3 * G + vb] = tVol;
+        b.part[4 * G + vb] = (double)tDel;
+        b.part[5 * G + vb] = (double)tBad;
     }
-    if (!last_block(&c->done[DC_CORRECT])) return;
+    if (!last_block(&c->done[DC_CORRECT], vg)) return;
     const double fErr = fold_partials(b.part + 0 * G, G, true, smem);
     const double fRad = fold_partials(b.part + 1 * G, G, true, smem);
     const double fExp = fold_partials(b.part + 2 * G, G, true, smem);
@@ -397,6 +401,8 @@ __global__ void __launch_bounds__(kBlock) k_correct(Bufs b) {
     if (threadIdx.x != 0) return;
     finish_attempt<DIM>(c, k, fErr, fRad, fExp, fVol, fDel, fBad);
 }
+CB_KERNEL_PAIR((template <int DIM>), k_correct, (<DIM>), __launch_bounds__(kBlock))
+
 
 // --------------------------------------------------------------- bootstrap
 // phase 0: pred := (x, r), vo := 0, path := 0
@@ -481,7 +487,7 @@ __global__ void __launch_bounds__(kBlock) k_energy(Bufs b, int per_bubble) {
     }
     const double t = block_reduce(tot, OpSum(), smem);
     if (threadIdx.x == 0) b.part[6 * gridDim.x + blockIdx.x] = t;
-    if (last_block(&c->done[DC_MISC])) {
+    if (last_block(&c->done[DC_MISC], gridDim.x)) {
         const double f = fold_partials(b.part + 6 * gridDim.x, gridDim.x, false, smem);
         if (threadIdx.x == 0) {
             c->misc_result = f;
@@ -506,7 +512,7 @@ __global__ void __launch_bounds__(kBlock) k_volume(Bufs b) {
     }
     const double t = block_reduce(tot, OpSum(), smem);
     if (threadIdx.x == 0) b.part[6 * gridDim.x + blockIdx.x] = t;
-    if (last_block(&c->done[DC_MISC])) {
+    if (last_block(&c->done[DC_MISC], gridDim.x)) {
         const double f = fold_partials(b.part + 6 * gridDim.x, gridDim.x, false, smem);
         if (threadIdx.x == 0) {
             c->misc_result = f;
@@ -519,17 +525,15 @@ __global__ void __launch_bounds__(kBlock) k_volume(Bufs b) {
 
 void launch_predict(const Launch &l, const Bufs &b, int dim) {
     if (dim == 3)
-        k_predict<3><<<wave_grid(k_predict<3>, l), kBlock, 0, l.stream>>>(b);
+        CB_LAUNCH(l, k_predict, (<3>), wave_grid(k_predict<3>, l), b);
     else
-        k_predict<2><<<wave_grid(k_predict<2>, l), kBlock, 0, l.stream>>>(b);
-    *l.launches += 1;
+        CB_LAUNCH(l, k_predict, (<2>), wave_grid(k_predict<2>, l), b);
 }
 
 // mode bits: 1 = gas exchange, 2 = flow. mode 0 is the bootstrap form.
 void launch_pairs(const Launch &l, const Bufs &b, int dim, int mode) {
     const bool gas = mode & 1, flow = mode & 2;
-#define CB_PAIRS(D, G, F) \
-    k_pairs<D, G, F><<<wave_grid(k_pairs<D, G, F>, l), kBlock, 0, l.stream>>>(b)
+#define CB_PAIRS(D, G, F) CB_LAUNCH(l, k_pairs, (<D, G, F>), wave_grid(k_pairs<D, G, F>, l), b)
     if (dim == 3) {
         if (gas && flow) CB_PAIRS(3, true, true);
         else if (gas) CB_PAIRS(3, true, false);
@@ -542,15 +546,13 @@ void launch_pairs(const Launch &l, const Bufs &b, int dim, int mode) {
         else CB_PAIRS(2, false, false);
     }
 #undef CB_PAIRS
-    *l.launches += 1;
 }
 
 void launch_correct(const Launch &l, const Bufs &b, int dim) {
     if (dim == 3)
-        k_correct<3><<<wave_grid(k_correct<3>, l), kBlock, 0, l.stream>>>(b);
+        CB_LAUNCH(l, k_correct, (<3>), wave_grid(k_correct<3>, l), b);
     else
-        k_correct<2><<<wave_grid(k_correct<2>, l), kBlock, 0, l.stream>>>(b);
-    *l.launches += 1;
+        CB_LAUNCH(l, k_correct, (<2>), wave_grid(k_correct<2>, l), b);
 }
 
 void launch_boot(const Launch &l, const Bufs &b, int dim, int phase) {

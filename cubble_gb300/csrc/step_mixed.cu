@@ -152,7 +152,7 @@ __device__ __forceinline__ void st_pred(const Bufs &b, int i, const PredMx &r) {
 
 // ---------------------------------------------------------------- predict
 template <int DIM>
-__global__ void __launch_bounds__(kBlock) k_predict_mx(Bufs b) {
+__device__ __forceinline__ void k_predict_mx_body(const Bufs &b, const int vb, const int vg) {
     __shared__ double smem[32];
     const Ctrl *c = b.ctrl;
     const int n = c->n;
@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(kBlock) k_predict_mx(Bufs b) {
     const float *O0 = frow(b, c, RVO0), *O1 = frow(b, c, RVO1), *O2 = frow(b, c, RVO2),
                 *O3 = frow(b, c, RVO3);
     float sA = 0.f, sAr = 0.f;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int i = vb * blockDim.x + threadIdx.x; i < n; i += vg * blockDim.x) {
         // AB2 increment h (3 v - vo) in FP32 on the fixed point of x
         PredMx p;
         p.q[0] = fix_from_double(X[i]) + fix_from_float(h * fmaf(3.f, V0[i], -O0[i]));
@@ -186,12 +186,12 @@ __global__ void __launch_bounds__(kBlock) k_predict_mx(Bufs b) {
     const double tA = block_sum_f(sA, smem);
     const double tAr = block_sum_f(sAr, smem);
     if (threadIdx.x == 0) {
-        b.part[0 * gridDim.x + blockIdx.x] = tA;
-        b.part[1 * gridDim.x + blockIdx.x] = tAr;
+        b.part[0 * vg + vb] = tA;
+        b.part[1 * vg + vb] = tAr;
     }
-    if (last_block(&b.ctrl->done[DC_PREDICT])) {
-        const double fA = fold_partials(b.part + 0 * gridDim.x, gridDim.x, false, smem);
-        const double fAr = fold_partials(b.part + 1 * gridDim.x, gridDim.x, false, smem);
+    if (last_block(&b.ctrl->done[DC_PREDICT], vg)) {
+        const double fA = fold_partials(b.part + 0 * vg, vg, false, smem);
+        const double fAr = fold_partials(b.part + 1 * vg, vg, false, smem);
         if (threadIdx.x == 0) {
             b.ctrl->sumA = fA;
             b.ctrl->sumAr = fAr;
@@ -199,6 +199,8 @@ __global__ void __launch_bounds__(kBlock) k_predict_mx(Bufs b) {
         }
     }
 }
+CB_KERNEL_PAIR((template <int DIM>), k_predict_mx, (<DIM>), __launch_bounds__(kBlock))
+
 
 // ------------------------------------------------------------------ pairs
 // The search emits the pairs grouped by i in ascending order, so consecutive
@@ -210,7 +212,7 @@ __global__ void __launch_bounds__(kBlock) k_predict_mx(Bufs b) {
 constexpr int kRun = 4;
 
 template <int DIM, bool GAS, bool FLOW>
-__global__ void __launch_bounds__(kBlock) k_pairs_mx(Bufs b) {
+__device__ __forceinline__ void k_pairs_mx_body(const Bufs &b, const int vb, const int vg) {
     __shared__ double smem[32];
     const Ctrl *c = b.ctrl;
     const DevConst &k = *b.k;
@@ -228,7 +230,7 @@ __global__ void __launch_bounds__(kBlock) k_pairs_mx(Bufs b) {
     const long long lx = k.lq[0], ly = k.lq[1], lz = k.lq[2];
     float sAo = 0.f, sAor = 0.f;
     const int nrun = (np + kRun - 1) / kRun;
-    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < nrun; g += gridDim.x * blockDim.x) {
+    for (int g = vb * blockDim.x + threadIdx.x; g < nrun; g += vg * blockDim.x) {
         const int p0 = g * kRun;
         int I[kRun], J[kRun];
         if (p0 + kRun <= np) {
@@ -334,12 +336,12 @@ __global__ void __launch_bounds__(kBlock) k_pairs_mx(Bufs b) {
     const double tAo = block_sum_f(sAo, smem);
     const double tAor = block_sum_f(sAor, smem);
     if (threadIdx.x == 0) {
-        b.part[2 * gridDim.x + blockIdx.x] = tAo;
-        b.part[3 * gridDim.x + blockIdx.x] = tAor;
+        b.part[2 * vg + vb] = tAo;
+        b.part[3 * vg + vb] = tAor;
     }
-    if (last_block(&b.ctrl->done[DC_PAIRS])) {
-        const double fAo = fold_partials(b.part + 2 * gridDim.x, gridDim.x, false, smem);
-        const double fAor = fold_partials(b.part + 3 * gridDim.x, gridDim.x, false, smem);
+    if (last_block(&b.ctrl->done[DC_PAIRS], vg)) {
+        const double fAo = fold_partials(b.part + 2 * vg, vg, false, smem);
+        const double fAor = fold_partials(b.part + 3 * vg, vg, false, smem);
         if (threadIdx.x == 0) {
             Ctrl *cc = b.ctrl;
             cc->sumAo = 2.0 * fAo;
@@ -351,6 +353,8 @@ __global__ void __launch_bounds__(kBlock) k_pairs_mx(Bufs b) {
         }
     }
 }
+CB_KERNEL_PAIR((template <int DIM, bool GAS, bool FLOW>), k_pairs_mx, (<DIM, GAS, FLOW>), __launch_bounds__(kBlock))
+
 
 // ---------------------------------------------------------------- correct
 // touchesWall, src/kernels.cu:553-566, on FP32 distances to both walls.
@@ -419,7 +423,7 @@ __device__ __forceinline__ CorrRed block_reduce_corr(CorrRed v, CorrRed *smem) {
 // to the control block with integer atomics (order-independent); only the
 // volume sum keeps per-block partials for its in-order FP64 fold.
 template <int DIM, bool GAS, bool FLOW, bool WALLS>
-__global__ void __launch_bounds__(kBlock, 4) k_correct_mx(Bufs b) {
+__device__ __forceinline__ void k_correct_mx_body(const Bufs &b, const int vb, const int vg) {
     __shared__ double smem[32];
     __shared__ CorrRed rsm[kBlock / 32];
     __shared__ unsigned long long tab[ND_ROLES];
@@ -445,7 +449,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_correct_mx(Bufs b) {
     float mexp = 0.f;
     double vol = 0.0;
     int ndel = 0, bad = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int i = vb * blockDim.x + threadIdx.x; i < n; i += vg * blockDim.x) {
         const float4 a = AV[i];
         float vpx = a.x, vpy = a.y, vpz = DIM == 3 ? a.z : 0.f, vpr = a.w;
         const float ovl = GAS ? (DIM == 3 ? AO[i] : a.z) : 0.f;  // overlap area sum
@@ -581,10 +585,10 @@ __global__ void __launch_bounds__(kBlock, 4) k_correct_mx(Bufs b) {
         atomicMax(&c->amax_exp, v.exp);
         if (v.del) atomicAdd(&c->acnt_del, v.del);
         if (v.bad) atomicAdd(&c->acnt_bad, v.bad);
-        b.part[blockIdx.x] = v.vol;
+        b.part[vb] = v.vol;
     }
-    if (!last_block(&c->done[DC_CORRECT])) return;
-    const double fVol = fold_partials(b.part, gridDim.x, false, smem);
+    if (!last_block(&c->done[DC_CORRECT], vg)) return;
+    const double fVol = fold_partials(b.part, vg, false, smem);
     if (threadIdx.x != 0) return;
     volatile Ctrl *vc = c;
     const double fErr = __longlong_as_double(vc->amax_err);
@@ -595,6 +599,8 @@ __global__ void __launch_bounds__(kBlock, 4) k_correct_mx(Bufs b) {
     c->acnt_del = c->acnt_bad = 0;
     finish_attempt<DIM>(c, k, fErr, fRad, fExp, fVol, fDel, fBad);
 }
+CB_KERNEL_PAIR((template <int DIM, bool GAS, bool FLOW, bool WALLS>), k_correct_mx, (<DIM, GAS, FLOW, WALLS>), __launch_bounds__(kBlock, 4))
+
 
 // --------------------------------------------------------------- bootstrap
 // phase 0: pred := fixed point of (x, r), vo := 0, path := 0
@@ -643,29 +649,31 @@ __global__ void __launch_bounds__(kBlock) k_boot_mx(Bufs b, int phase) {
 template <int DIM, bool GAS>
 void launch_correct_mx_t(const Launch &l, const Bufs &b, bool flow, bool walls) {
     if (flow && walls)
-        k_correct_mx<DIM, GAS, true, true><<<wave_grid(k_correct_mx<DIM, GAS, true, true>, l), kBlock, 0, l.stream>>>(b);
+        CB_LAUNCH(l, k_correct_mx, (<DIM, GAS, true, true>),
+                  wave_grid(k_correct_mx<DIM, GAS, true, true>, l), b);
     else if (flow)
-        k_correct_mx<DIM, GAS, true, false><<<wave_grid(k_correct_mx<DIM, GAS, true, false>, l), kBlock, 0, l.stream>>>(b);
+        CB_LAUNCH(l, k_correct_mx, (<DIM, GAS, true, false>),
+                  wave_grid(k_correct_mx<DIM, GAS, true, false>, l), b);
     else if (walls)
-        k_correct_mx<DIM, GAS, false, true><<<wave_grid(k_correct_mx<DIM, GAS, false, true>, l), kBlock, 0, l.stream>>>(b);
+        CB_LAUNCH(l, k_correct_mx, (<DIM, GAS, false, true>),
+                  wave_grid(k_correct_mx<DIM, GAS, false, true>, l), b);
     else
-        k_correct_mx<DIM, GAS, false, false><<<wave_grid(k_correct_mx<DIM, GAS, false, false>, l), kBlock, 0, l.stream>>>(b);
+        CB_LAUNCH(l, k_correct_mx, (<DIM, GAS, false, false>),
+                  wave_grid(k_correct_mx<DIM, GAS, false, false>, l), b);
 }
 
 }  // namespace
 
 void launch_predict_mx(const Launch &l, const Bufs &b, int dim) {
     if (dim == 3)
-        k_predict_mx<3><<<wave_grid(k_predict_mx<3>, l), kBlock, 0, l.stream>>>(b);
+        CB_LAUNCH(l, k_predict_mx, (<3>), wave_grid(k_predict_mx<3>, l), b);
     else
-        k_predict_mx<2><<<wave_grid(k_predict_mx<2>, l), kBlock, 0, l.stream>>>(b);
-    *l.launches += 1;
+        CB_LAUNCH(l, k_predict_mx, (<2>), wave_grid(k_predict_mx<2>, l), b);
 }
 
 void launch_pairs_mx(const Launch &l, const Bufs &b, int dim, int mode) {
     const bool gas = mode & 1, flow = mode & 2;
-#define CB_PAIRS(D, G, F) \
-    k_pairs_mx<D, G, F><<<wave_grid(k_pairs_mx<D, G, F>, l), kBlock, 0, l.stream>>>(b)
+#define CB_PAIRS(D, G, F) CB_LAUNCH(l, k_pairs_mx, (<D, G, F>), wave_grid(k_pairs_mx<D, G, F>, l), b)
     if (dim == 3) {
         if (gas && flow) CB_PAIRS(3, true, true);
         else if (gas) CB_PAIRS(3, true, false);
@@ -678,7 +686,6 @@ void launch_pairs_mx(const Launch &l, const Bufs &b, int dim, int mode) {
         else CB_PAIRS(2, false, false);
     }
 #undef CB_PAIRS
-    *l.launches += 1;
 }
 
 void launch_correct_mx(const Launch &l, const Bufs &b, int dim, int mode, bool walls) {
@@ -694,7 +701,6 @@ void launch_correct_mx(const Launch &l, const Bufs &b, int dim, int mode, bool w
         else
             launch_correct_mx_t<2, false>(l, b, flow, walls);
     }
-    *l.launches += 1;
 }
 
 void launch_boot_mx(const Launch &l, const Bufs &b, int dim, int phase) {
