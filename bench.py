@@ -363,6 +363,112 @@ def mixed_errors(args, steps=50):
     return out
 
 
+def batch_errors(items, steps=50):
+    """Mixed batch against the FP64 batch of the same foams from the same
+    FP64-prepared state (positions, rates, pairs, dt): max over foams of the
+    displacement-relative position error, the radius error and the total
+    volume drift after `steps` accepted steps."""
+    import cubble_gb300 as cb
+    from cubble_gb300 import workloads
+    cf64 = [c for c, _ in items]
+    cfmx = [workloads.sweep_config_as(c, precision=1) for c in cf64]
+    b64, bmx = cb.GpuFoamBatch(cf64), cb.GpuFoamBatch(cfmx)
+    s0 = []
+    for (cfg, st), f64, fmx in zip(items, b64.foams, bmx.foams):
+        f64.load_state(st)
+        workloads.prepare(f64)
+        s = f64.get_state()
+        i, j = f64.pairs()
+        fmx.load_state(s)
+        fmx.set_pairs(i, j)
+        fmx.set_time(f64.report()["time_step"])
+        s0.append(s)
+    r64, rmx = b64.integrate(steps), bmx.integrate(steps)
+    out = {"steps": steps, "foams": len(items), "same_attempts_searches_deletions": True,
+           "dx": 0.0, "r": 0.0, "volume_drift": 0.0}
+    for f, ((cfg, _), f64, fmx) in enumerate(zip(items, b64.foams, bmx.foams)):
+        if any(r64[f][k] != rmx[f][k] for k in ("attempts", "searches", "deleted")):
+            out["same_attempts_searches_deletions"] = False
+        a, b = f64.get_state(), fmx.get_state()
+        order_a, order_b = np.argsort(a["index"]), np.argsort(b["index"])
+        o0 = np.argsort(s0[f]["index"])
+        for ax, k in enumerate(("x", "y")):
+            L = cfg.tfr[ax] - cfg.lbb[ax]
+            d = b[k][order_b] - a[k][order_a]
+            d -= L * np.round(d / L)
+            m = a[k][order_a] - s0[f][k][o0]
+            m -= L * np.round(m / L)
+            out["dx"] = max(out["dx"], float(np.max(np.abs(d)) / max(np.max(np.abs(m)), 1e-300)))
+        out["r"] = max(out["r"], float(np.max(np.abs(b["r"][order_b] - a["r"][order_a])) /
+                                        np.max(np.abs(a["r"]))))
+        v64, vmx = f64.total_volume(), fmx.total_volume()
+        out["volume_drift"] = max(out["volume_drift"], abs(vmx - v64) / v64)
+    b64.close()
+    bmx.close()
+    return out
+
+
+def measure_batch(args, world, rank):
+    """The batched parameter sweep: `--batch-count` independent 2D periodic
+    foams (N log-uniform in [1e3, 1e5], phi in [0.85, 0.95], kappa
+    log-uniform in [1e-3, 1e-1]) in the mixed form, all advanced by one
+    graph launch per call, tile picked by the autotuner."""
+    import torch
+    import cubble_gb300 as cb
+    from cubble_gb300 import workloads
+    items = workloads.sweep(count=args.batch_count, seed=4 + 1000 * rank, precision=1,
+                            use_graph=1)
+    t0 = time.perf_counter()
+    batch = cb.GpuFoamBatch([c for c, _ in items])
+    for (cfg, st), f in zip(items, batch.foams):
+        f.load_state(st)
+        workloads.prepare(f)
+    setup_s = time.perf_counter() - t0
+    tile = batch.autotune(args.batch_tune_steps)
+    batch.integrate(args.warmup)
+    r0 = [f.report() for f in batch.foams]
+    l0 = batch.launch_count()
+    barrier(world)
+    torch.cuda.synchronize()
+    reps, ms = batch.integrate_timed(args.batch_steps)
+    torch.cuda.synchronize()
+    barrier(world)
+    launches = batch.launch_count() - l0
+    bs = sum(r["bubble_steps"] - q["bubble_steps"] for r, q in zip(reps, r0))
+    el = allreduce(ms / 1e3, _op("max"), world)
+    bs_all = allreduce(bs, _op("sum"), world)
+    n_now = sum(r["count"] for r in reps)
+    np_now = sum(r["num_pairs"] for r in reps)
+    ab = algorithmic_bytes(2, np_now / max(n_now, 1), mixed=True)
+    value = bs_all / el
+    hbm, src = peaks()
+    achieved = ab["step"] * bs / (ms / 1e3) / 1e9
+    out = {"value": value, "unit": "bubble-steps/s",
+           "ms_per_batch_step": ms / args.batch_steps,
+           "foams": len(items), "bubbles": int(sum(st["x"].size for _, st in items)),
+           "steps_each": args.batch_steps, "tile_bubbles_per_block": tile,
+           "attempts": sum(r["attempts"] - q["attempts"] for r, q in zip(reps, r0)),
+           "searches": sum(r["searches"] - q["searches"] for r, q in zip(reps, r0)),
+           "deleted": sum(r["deleted"] - q["deleted"] for r, q in zip(reps, r0)),
+           "gpu_launches": launches, "setup_s": setup_s,
+           "roofline": {"bound": "hbm", "kernel": "whole batched step",
+                        "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                        "frac": achieved / hbm,
+                        "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs)",
+                        "algorithmic_bytes_per_bubble_step": ab["step"]},
+           "workload": "%d independent 2D periodic foams, N log-uniform in [1e3, 1e5] "
+                       "(seeded), phi U[0.85, 0.95], kappa log-uniform [1e-3, 1e-1], "
+                       "r~N(1, 0.1) in [0.3, 2.0], mixed precision, one graph launch, "
+                       "autotuned tile" % len(items)}
+    batch.close()
+    if rank == 0:
+        pick = sorted(range(len(items)), key=lambda f: items[f][1]["x"].size)
+        sub = [items[f] for f in pick[:: max(1, len(pick) // 4)][:4]]
+        sub = [(workloads.sweep_config_as(c, precision=0), st) for c, st in sub]
+        out["error_vs_fp64"] = batch_errors(sub)
+    return out
+
+
 def run_gb300(args, world, rank, local):
     import torch
     import cubble_gb300 as cb
@@ -422,6 +528,10 @@ def run_gb300(args, world, rank, local):
         if rank == 0:
             mixed["error_vs_fp64"] = mixed_errors(args)
 
+    batched = None
+    if not args.no_batch:
+        batched = measure_batch(args, world, rank)
+
     base = None
     if rank == 0 and not args.no_cpu:
         v, cores, n_steps, secs = cpu_baseline(cfg, st, args.cpu_steps)
@@ -444,6 +554,7 @@ def run_gb300(args, world, rank, local):
                    "deleted": r1["deleted"] - r0["deleted"], "dt_end": r1["time_step"]},
         "roofline": main["roofline"], "cpu_baseline": base, "e2e": e2e,
         "gpu_launches": main["launches"], "clocks": main["clocks"], "mixed": mixed,
+        "batched": batched,
     }
     print(json.dumps(line))
 
@@ -471,6 +582,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-count", type=int, default=256)
+    ap.add_argument("--batch-steps", type=int, default=300)
+    ap.add_argument("--batch-tune-steps", type=int, default=10)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

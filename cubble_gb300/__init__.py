@@ -64,3 +64,85 @@ class GpuFoam(Foam):
         n = C.c_int64()
         self._call("launch_count", self._ctx, C.byref(n))
         return n.value
+
+
+class _BatchFoam(GpuFoam):
+    """A foam owned by a GpuFoamBatch (its context lives as long as the batch)."""
+
+    def __init__(self, batch, index, config):
+        self._lib = batch._lib
+        self._p = "cb_"
+        self.config = config
+        self._batch = batch  # keeps the batch alive
+        self._ctx = C.c_void_p()
+        batch._call("batch_context", batch._b, int(index), C.byref(self._ctx))
+
+    def close(self):
+        self._ctx = C.c_void_p()
+
+
+class GpuFoamBatch:
+    """Independent foams advanced together, one launch per stage for all of
+    them (a `cb_batch`). `foams[f]` is foam f's single-foam interface (load
+    its state, search, bootstrap, read it back); `integrate(n)` advances
+    every foam by n accepted steps."""
+
+    def __init__(self, configs):
+        self._lib = lib()
+        self._b = C.c_void_p()
+        arr = (_abi.Config * len(configs))(*configs)
+        self._call("batch_create", arr, len(configs), C.byref(self._b))
+        self.foams = [_BatchFoam(self, f, cfg) for f, cfg in enumerate(configs)]
+
+    def _call(self, name, *args):
+        rc = getattr(self._lib, "cb_" + name)(*args)
+        if rc != 0:
+            msg = self._lib.cb_last_error()
+            raise CubbleError(rc, msg.decode() if msg else "")
+        return rc
+
+    def __len__(self):
+        return len(self.foams)
+
+    def integrate(self, n_steps=1):
+        reps = (_abi.Report * len(self.foams))()
+        self._call("batch_integrate", self._b, int(n_steps), reps)
+        return [r.as_dict() for r in reps]
+
+    def integrate_timed(self, n_steps):
+        reps = (_abi.Report * len(self.foams))()
+        ms = C.c_double()
+        self._call("batch_integrate_timed", self._b, int(n_steps), reps, C.byref(ms))
+        return [r.as_dict() for r in reps], ms.value
+
+    def set_tile(self, bubbles_per_block):
+        self._call("batch_set_tile", self._b, int(bubbles_per_block))
+
+    def autotune(self, steps_per_trial):
+        t = C.c_int32()
+        self._call("batch_autotune", self._b, int(steps_per_trial), C.byref(t))
+        return t.value
+
+    def launch_count(self):
+        n = C.c_int64()
+        self._call("batch_launch_count", self._b, C.byref(n))
+        return n.value
+
+    def close(self):
+        if self._b:
+            for f in self.foams:
+                f.close()
+            self._lib.cb_batch_destroy(self._b)
+            self._b = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

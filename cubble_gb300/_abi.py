@@ -143,6 +143,15 @@ def declare(lib, prefix):
             "profile_kernels": (C.c_int, [vp, C.c_int32, C.POINTER(C.c_double)]),
             "energy_noalloc": (C.c_int, [C.POINTER(Config), vp, vp, vp, vp, vp, vp,
                                          C.c_int32, C.c_int32, vp, vp]),
+            "batch_create": (C.c_int, [C.POINTER(Config), C.c_int32, C.POINTER(vp)]),
+            "batch_destroy": (C.c_int, [vp]),
+            "batch_context": (C.c_int, [vp, C.c_int32, C.POINTER(vp)]),
+            "batch_integrate": (C.c_int, [vp, C.c_int64, C.POINTER(Report)]),
+            "batch_integrate_timed": (C.c_int, [vp, C.c_int64, C.POINTER(Report),
+                                                C.POINTER(C.c_double)]),
+            "batch_set_tile": (C.c_int, [vp, C.c_int32]),
+            "batch_autotune": (C.c_int, [vp, C.c_int32, C.POINTER(C.c_int32)]),
+            "batch_launch_count": (C.c_int, [vp, C.POINTER(C.c_int64)]),
         },
         "cbo_": {
             "set_threads": (C.c_int, [vp, C.c_int32]),

@@ -110,8 +110,8 @@ struct Ctrl {
     int acnt_del, acnt_bad;
     // Batched launches (several foams per launch): which phases this foam
     // takes part in next (BatchSel bits, set between launches) and the
-    // number of blocks of its virtual grid.
-    int bsel, vgrid;
+    // blocks of its virtual grid in the attempt and in the search / deletion.
+    int bsel, vgrid_a, vgrid_s;
     unsigned int done[DC_COUNT];
 };
 
@@ -437,52 +437,67 @@ struct Launch {
     cudaStream_t stream;
     long long *launches;  // host-side launch counter
     // Batched launches: when `batch` is set, every launcher runs its kernel's
-    // batched form over `count` foams (device table of their Bufs) on a
-    // dim3(gmax, count) grid, for the foams whose Ctrl::bsel has `sel`.
+    // batched form over the work list `work` (device) of the foams in the
+    // device table `batch`, on a 1D grid of `gmax` blocks.
     const struct Bufs *batch = nullptr;
-    int count = 0, gmax = 0, sel = 0;
+    const struct BatchWork *work = nullptr;
+    int gmax = 0;
 };
 
 // Phases of a batched step a foam takes part in (Ctrl::bsel bits).
 enum BatchSel : int { SEL_ATTEMPT = 1, SEL_DELETE = 2, SEL_SEARCH = 4 };
 
-// Batched form of a kernel: blockIdx.y picks the foam; its blocks
-// 0 .. vgrid-1 run the body with (vb, vg) = (blockIdx.x, vgrid) in place of
-// (blockIdx.x, gridDim.x); the other blocks, and every block of a foam that
-// is not selected, return at once. Returns false for those.
-__device__ __forceinline__ bool batch_slot(const Bufs *bb, int sel, Bufs &b, int &vb, int &vg) {
-    const Ctrl *c = bb[blockIdx.y].ctrl;
-    if (!(c->bsel & sel)) return false;
-    vg = c->vgrid;
-    if ((int)blockIdx.x >= vg) return false;
-    vb = blockIdx.x;
-    b = bb[blockIdx.y];
-    return true;
+// Work list of one batched phase: the selected foams and the prefix sums of
+// their virtual grids; work item w belongs to the foam k with
+// pre[k] <= w < pre[k + 1] and is its block w - pre[k].
+struct BatchWork {
+    int nsel, total;
+    int *foam;  // nsel entries
+    int *pre;   // nsel + 1 entries
+};
+
+__device__ __forceinline__ int batch_item(const BatchWork *wk, int item, int &vb, int &vg) {
+    const int *pre = wk->pre;
+    int lo = 0, hi = wk->nsel - 1;  // largest k with pre[k] <= item
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (pre[mid] <= item)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    vb = item - pre[lo];
+    vg = pre[lo + 1] - pre[lo];
+    return wk->foam[lo];
 }
 
 #define CB_ID(...) __VA_ARGS__
 
 // Declares the single-foam kernel NAME(Bufs) and its batched form
-// NAME_batch(const Bufs *, int sel) around the body NAME_body(b, vb, vg).
+// NAME_batch(const Bufs *, const BatchWork *) around the body
+// NAME_body(b, vb, vg): the batched form loops over the phase's work items
+// on a fixed grid (no block waits for another).
 // TPL is the parenthesised template header ("(template <int DIM>)" or "()"),
 // ARGS the parenthesised template arguments ("(<DIM>)" or "()").
 #define CB_KERNEL_PAIR(TPL, NAME, ARGS, BOUNDS)                                  \
     CB_ID TPL __global__ void BOUNDS NAME(Bufs b) {                                \
         NAME##_body CB_ID ARGS(b, blockIdx.x, gridDim.x);                          \
     }                                                                              \
-    CB_ID TPL __global__ void BOUNDS NAME##_batch(const Bufs *bb, int sel) {       \
-        Bufs b;                                                                    \
-        int vb, vg;                                                                \
-        if (!batch_slot(bb, sel, b, vb, vg)) return;                               \
-        NAME##_body CB_ID ARGS(b, vb, vg);                                         \
+    CB_ID TPL __global__ void BOUNDS NAME##_batch(const Bufs *bb, const BatchWork *wk) { \
+        const int total = wk->total;                                               \
+        for (int item = blockIdx.x; item < total; item += gridDim.x) {             \
+            int vb, vg;                                                            \
+            const Bufs b = bb[batch_item(wk, item, vb, vg)];                       \
+            NAME##_body CB_ID ARGS(b, vb, vg);                                     \
+            __syncthreads();                                                       \
+        }                                                                          \
     }
 
 // Launches NAME<ARGS> in its single or batched form per the Launch `l`.
 #define CB_LAUNCH(l, NAME, ARGS, GRID, b)                                             \
     do {                                                                             \
         if ((l).batch)                                                               \
-            NAME##_batch CB_ID ARGS<<<dim3((l).gmax, (l).count), kBlock, 0, (l).stream>>>( \
-                (l).batch, (l).sel);                                                 \
+            NAME##_batch CB_ID ARGS<<<(l).gmax, kBlock, 0, (l).stream>>>((l).batch, (l).work); \
         else                                                                         \
             NAME CB_ID ARGS<<<(GRID), kBlock, 0, (l).stream>>>(b);                   \
         *(l).launches += 1;                                                          \

@@ -10,25 +10,19 @@
 #include <string>
 #include <vector>
 
-#include "common.cuh"
+#include "context.cuh"
 
 using namespace cbg;
 
 namespace {
-
 thread_local std::string g_err;
+}  // namespace
 
+namespace cbg {
 int fail(int code, const std::string &msg) {
     g_err = msg;
     return code;
 }
-
-#define CB_CUDA(x)                                                                          \
-    do {                                                                                    \
-        cudaError_t e_ = (x);                                                               \
-        if (e_ != cudaSuccess)                                                              \
-            return fail(CB_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));      \
-    } while (0)
 
 const char *status_text(int s) {
     switch (s) {
@@ -41,71 +35,9 @@ const char *status_text(int s) {
     }
 }
 
-// Kernels per phase (for the launch counter of graph executions).
-constexpr int kKernelsPerAttempt = 3;
-constexpr int kKernelsPerRemove = 9;
-constexpr int kKernelsPerSearch = 15;
-
-}  // namespace
-
-namespace cbg {
 void set_last_error(const std::string &msg) { g_err = msg; }
 }  // namespace cbg
 
-struct cb_context {
-    cb_config cfg{};
-    int dev = 0, sms = 0;
-    cudaStream_t stream = nullptr;
-    DevConst hk{};
-    DevConst *dk = nullptr;
-    Ctrl *dctrl = nullptr;
-    Ctrl *hctrl = nullptr;  // pinned mirror
-    std::vector<void *> allocs;
-    double *dslot[ND_ROLES] = {};
-    int *islot[NI_ROLES] = {};
-    int *pslot[NP_ROLES] = {};
-    double **d_dslots = nullptr;
-    int **d_islots = nullptr;
-    int **d_pslots = nullptr;
-    Bufs bufs{};
-    Launch launch{};
-    long long launches = 0;
-    bool loaded = false;
-    cudaGraphExec_t gexec = nullptr;
-    int graph_key = -1;
-    long long graph_attempts0 = 0, graph_searches0 = 0, graph_deletes0 = 0;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-
-    template <typename T>
-    int alloc(T **p, size_t n) {
-        void *q = nullptr;
-        CB_CUDA(cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T)));
-        CB_CUDA(cudaMemsetAsync(q, 0, std::max<size_t>(n, 1) * sizeof(T), stream));
-        allocs.push_back(q);
-        *p = static_cast<T *>(q);
-        return CB_OK;
-    }
-    int pull() {
-        CB_CUDA(cudaMemcpyAsync(hctrl, dctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, stream));
-        CB_CUDA(cudaStreamSynchronize(stream));
-        return CB_OK;
-    }
-    int push() {
-        CB_CUDA(cudaMemcpyAsync(dctrl, hctrl, sizeof(Ctrl), cudaMemcpyHostToDevice, stream));
-        CB_CUDA(cudaStreamSynchronize(stream));
-        return CB_OK;
-    }
-    int upload_const() {
-        CB_CUDA(cudaMemcpyAsync(dk, &hk, sizeof(DevConst), cudaMemcpyHostToDevice, stream));
-        CB_CUDA(cudaStreamSynchronize(stream));
-        return CB_OK;
-    }
-    int mode() const { return (hctrl->use_gas ? 1 : 0) | (hctrl->use_flow ? 2 : 0); }
-    int check_launch() {
-        CB_CUDA(cudaGetLastError());
-        return CB_OK;
-    }
-};
 
 namespace {
 
@@ -157,6 +89,9 @@ void fill_const(cb_context *c) {
     k.pre_margin = (float)(1e-5 * (maxabs + maxiv) + 1e-4);
 }
 
+}  // namespace
+
+namespace cbg {
 int sync_status(cb_context *c) {
     int rc = c->pull();
     if (rc) return rc;
@@ -165,7 +100,7 @@ int sync_status(cb_context *c) {
 }
 
 // The three kernels of one step() attempt, in the context's precision.
-void launch_attempt_kernels(const cb_context *c, const Launch &l, const Bufs &b, int which = 7) {
+void launch_attempt_kernels(const cb_context *c, const Launch &l, const Bufs &b, int which) {
     const int dim = c->hk.dim;
     if (c->hk.mixed) {
         if (which & 1) launch_predict_mx(l, b, dim);
@@ -177,6 +112,10 @@ void launch_attempt_kernels(const cb_context *c, const Launch &l, const Bufs &b,
         if (which & 4) launch_correct(l, b, dim);
     }
 }
+
+}  // namespace cbg
+
+namespace {
 
 int run_attempt(cb_context *c) {
     launch_attempt_kernels(c, c->launch, c->bufs);
@@ -213,6 +152,9 @@ int integrate_eager(cb_context *c, int64_t n_steps) {
     return sync_status(c);
 }
 
+}  // namespace
+
+namespace cbg {
 // Adds a conditional node to the graph that `stream` is capturing into and
 // returns its body graph; the capture continues after the node.
 int capture_conditional(cudaStream_t stream, cudaGraphConditionalNodeType type,
@@ -237,6 +179,10 @@ int capture_conditional(cudaStream_t stream, cudaGraphConditionalNodeType type,
     *body = p.conditional.phGraph_out[0];
     return CB_OK;
 }
+
+}  // namespace cbg
+
+namespace {
 
 // integrate(n) as one graph:
 //   WHILE(h_loop) { predict; pairs; correct; IF(h_delete) remove; IF(h_search) search }
@@ -318,6 +264,9 @@ int integrate_graph(cb_context *c, int64_t n_steps) {
     return CB_OK;
 }
 
+}  // namespace
+
+namespace cbg {
 void fill_report(const cb_context *c, cb_report *r) {
     const Ctrl &h = *c->hctrl;
     std::memset(r, 0, sizeof(*r));
@@ -336,6 +285,10 @@ void fill_report(const cb_context *c, cb_report *r) {
     r->num_pairs = h.np;
     r->status = h.status;
 }
+
+}  // namespace cbg
+
+namespace {
 
 }  // namespace
 

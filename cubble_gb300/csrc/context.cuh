@@ -1,0 +1,93 @@
+// Host-side internals shared by the single-foam context (context.cu) and
+// the batched foams (batch.cu). Not part of the C ABI.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace cbg {
+int fail(int code, const std::string &msg);
+const char *status_text(int s);
+// Kernels per phase (for the launch counter of graph executions).
+constexpr int kKernelsPerAttempt = 3;
+constexpr int kKernelsPerRemove = 9;
+constexpr int kKernelsPerSearch = 15;
+}  // namespace cbg
+
+#define CB_CUDA(x)                                                                          \
+    do {                                                                                    \
+        cudaError_t e_ = (x);                                                               \
+        if (e_ != cudaSuccess)                                                              \
+            return cbg::fail(CB_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));      \
+    } while (0)
+
+using cbg::Bufs;
+using cbg::Ctrl;
+using cbg::DevConst;
+using cbg::Launch;
+
+struct cb_context {
+    cb_config cfg{};
+    int dev = 0, sms = 0;
+    cudaStream_t stream = nullptr;
+    DevConst hk{};
+    DevConst *dk = nullptr;
+    Ctrl *dctrl = nullptr;
+    Ctrl *hctrl = nullptr;  // pinned mirror
+    std::vector<void *> allocs;
+    double *dslot[cbg::ND_ROLES] = {};
+    int *islot[cbg::NI_ROLES] = {};
+    int *pslot[cbg::NP_ROLES] = {};
+    double **d_dslots = nullptr;
+    int **d_islots = nullptr;
+    int **d_pslots = nullptr;
+    Bufs bufs{};
+    Launch launch{};
+    long long launches = 0;
+    bool loaded = false;
+    cudaGraphExec_t gexec = nullptr;
+    int graph_key = -1;
+    long long graph_attempts0 = 0, graph_searches0 = 0, graph_deletes0 = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    template <typename T>
+    int alloc(T **p, size_t n) {
+        void *q = nullptr;
+        CB_CUDA(cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T)));
+        CB_CUDA(cudaMemsetAsync(q, 0, std::max<size_t>(n, 1) * sizeof(T), stream));
+        allocs.push_back(q);
+        *p = static_cast<T *>(q);
+        return CB_OK;
+    }
+    int pull() {
+        CB_CUDA(cudaMemcpyAsync(hctrl, dctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, stream));
+        CB_CUDA(cudaStreamSynchronize(stream));
+        return CB_OK;
+    }
+    int push() {
+        CB_CUDA(cudaMemcpyAsync(dctrl, hctrl, sizeof(Ctrl), cudaMemcpyHostToDevice, stream));
+        CB_CUDA(cudaStreamSynchronize(stream));
+        return CB_OK;
+    }
+    int upload_const() {
+        CB_CUDA(cudaMemcpyAsync(dk, &hk, sizeof(DevConst), cudaMemcpyHostToDevice, stream));
+        CB_CUDA(cudaStreamSynchronize(stream));
+        return CB_OK;
+    }
+    int mode() const { return (hctrl->use_gas ? 1 : 0) | (hctrl->use_flow ? 2 : 0); }
+    int check_launch() {
+        CB_CUDA(cudaGetLastError());
+        return CB_OK;
+    }
+};
+
+namespace cbg {
+int sync_status(cb_context *c);
+void launch_attempt_kernels(const cb_context *c, const Launch &l, const Bufs &b, int which = 7);
+int capture_conditional(cudaStream_t stream, cudaGraphConditionalNodeType type,
+                        cudaGraphConditionalHandle *handle, unsigned int dflt,
+                        cudaGraph_t *body);
+void fill_report(const cb_context *c, cb_report *r);
+}  // namespace cbg

@@ -97,11 +97,12 @@ __global__ void __launch_bounds__(1024) k_scan_top(int *blocksums, int nblocks) 
     k_scan_top_body(blocksums, nblocks);
 }
 
-// Batched form: one block per selected foam, over its virtual grid's sums.
-__global__ void __launch_bounds__(1024) k_scan_top_batch(const Bufs *bb, int sel) {
-    const Bufs &b = bb[blockIdx.y];
-    if (!(b.ctrl->bsel & sel)) return;
-    k_scan_top_body(b.blocksums, b.ctrl->vgrid);
+// Batched form: the selected foams in turn, over their virtual grids' sums.
+__global__ void __launch_bounds__(1024) k_scan_top_batch(const Bufs *bb, const BatchWork *wk) {
+    for (int k = blockIdx.x; k < wk->nsel; k += gridDim.x) {
+        k_scan_top_body(bb[wk->foam[k]].blocksums, wk->pre[k + 1] - wk->pre[k]);
+        __syncthreads();
+    }
 }
 
 template <int KIND>
@@ -137,7 +138,7 @@ template <int KIND>
 void launch_scan_t(const Launch &l, const Bufs &b) {
     CB_LAUNCH(l, k_scan_sums, (<KIND>), l.scan_grid, b);
     if (l.batch)
-        k_scan_top_batch<<<dim3(1, l.count), 1024, 0, l.stream>>>(l.batch, l.sel);
+        k_scan_top_batch<<<l.sms, 1024, 0, l.stream>>>(l.batch, l.work);
     else
         k_scan_top<<<1, 1024, 0, l.stream>>>(b.blocksums, l.scan_grid);
     *l.launches += 1;

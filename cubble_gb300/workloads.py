@@ -75,3 +75,32 @@ def prepare(sim):
     (src/simulator.cu:720-787)."""
     sim.search_neighbors()
     sim.bootstrap()
+
+
+def sweep(count=256, seed=4, n_range=(1_000, 100_000), phi_range=(0.85, 0.95),
+          kappa_range=(1e-3, 1e-1), **kw):
+    """The batched parameter sweep: `count` independent 2D periodic foams,
+    N log-uniform in n_range, phi uniform in phi_range, kappa log-uniform in
+    kappa_range, r ~ N(1, 0.1) clipped to [0.3, 2.0], K=0.1, tol 1e-5,
+    min_rad 0.05. Returns a list of (config, state), one per foam, each
+    foam from its own seed."""
+    rng = np.random.default_rng(seed)
+    lo, hi = math.log(n_range[0]), math.log(n_range[1])
+    out = []
+    for f in range(count):
+        n = int(round(math.exp(rng.uniform(lo, hi))))
+        phi = float(rng.uniform(*phi_range))
+        kappa = float(math.exp(rng.uniform(math.log(kappa_range[0]),
+                                           math.log(kappa_range[1]))))
+        out.append(foam(n, 2, phi, 1.0, 0.1, (0.3, 2.0), seed=seed * 100003 + f,
+                        kappa=kappa, k_param=0.1, min_rad=0.05, **kw))
+    return out
+
+
+def sweep_config_as(cfg, **changes):
+    """A copy of a config with some fields changed (e.g. the precision)."""
+    import copy
+    c = copy.copy(cfg)
+    for k, v in changes.items():
+        setattr(c, k, v)
+    return c

@@ -212,6 +212,41 @@ CB_API int cb_profile_kernels(cb_context *ctx, int32_t reps, double ms[3]);
  * kernel nodes are counted per execution). */
 CB_API int cb_launch_count(cb_context *ctx, int64_t *count);
 
+/* ------------------------------------------------------------ batches
+ * Many independent foams advanced together: the array-job parameter sweep
+ * (scripts/triton/array_job.py:54-75 submits one simulate() process per
+ * parameter set) as one device job. Every stage of integrate() is one launch
+ * over all foams (foam f runs on a virtual grid sized to its capacity), the
+ * step loop is one CUDA graph, and each foam keeps its own adaptive dt,
+ * accept/reject, search and deletion exactly as a cb_context running
+ * integrate() alone. The reference has no batched form.
+ *
+ * All configs must agree on dimensionality, precision, use_gas_exchange,
+ * use_flow and whether any wall is set; capacities and every other
+ * parameter may differ. Each foam is a cb_context owned by the batch
+ * (cb_batch_context): load its state, search and bootstrap it through the
+ * single-foam calls, then advance all foams with cb_batch_integrate. */
+typedef struct cb_batch cb_batch;
+CB_API int cb_batch_create(const cb_config *configs, int32_t count, cb_batch **out);
+CB_API int cb_batch_destroy(cb_batch *batch);
+/* The context of foam `index` (owned by the batch; do not cb_destroy it). */
+CB_API int cb_batch_context(cb_batch *batch, int32_t index, cb_context **ctx);
+/* n_steps accepted steps of every foam whose status is CB_OK; reports[f]
+ * (count entries, may be NULL) receives foam f's report. Returns the first
+ * foam's error, if any foam's status is not CB_OK at the end. */
+CB_API int cb_batch_integrate(cb_batch *batch, int64_t n_steps, cb_report *reports);
+/* As cb_batch_integrate; *ms = device time of the whole job (CUDA events). */
+CB_API int cb_batch_integrate_timed(cb_batch *batch, int64_t n_steps, cb_report *reports,
+                                    double *ms);
+/* Bubbles per block of every foam's virtual grid (a multiple of 256,
+ * >= 256); the default is 2048. */
+CB_API int cb_batch_set_tile(cb_batch *batch, int32_t bubbles_per_block);
+/* Autotuner: times `steps_per_trial` steps (these advance the foams) with
+ * each candidate tile (512 ... 8192 bubbles per block), keeps the fastest
+ * and returns it in *tile. */
+CB_API int cb_batch_autotune(cb_batch *batch, int32_t steps_per_trial, int32_t *tile);
+CB_API int cb_batch_launch_count(cb_batch *batch, int64_t *count);
+
 /* Total potential energy of a foam, as cb_energy computes it, for callers
  * that cannot allocate device memory. No counterpart in the reference.
  *
