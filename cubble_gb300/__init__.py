@@ -65,6 +65,51 @@ class GpuFoam(Foam):
         self._call("launch_count", self._ctx, C.byref(n))
         return n.value
 
+    def integrate_until(self, max_steps, time=None, min_count=-1, max_radius=float("inf")):
+        """Up to max_steps accepted steps, ending after the first one that
+        reaches `time` (the simulation clock), leaves <= min_count bubbles
+        or makes the largest radius >= max_radius."""
+        st = _abi.Stop()
+        t = float("inf") if time is None else float(time)
+        if t == float("inf"):
+            st.time_integer, st.time_fraction = (1 << 63), 0.0
+        else:
+            st.time_integer = int(t)
+            st.time_fraction = t - int(t)
+        st.min_count = int(min_count)
+        st.max_radius = float(max_radius)
+        r = _abi.Report()
+        self._call("integrate_until", self._ctx, int(max_steps), C.byref(st), C.byref(r))
+        return r.as_dict()
+
+    def transform_positions(self, normalize):
+        self._call("transform_positions", self._ctx, 1 if normalize else 0)
+
+    def averages(self):
+        """Means of r, dxdt, dydt, dzdt, drdt, path."""
+        out = (C.c_double * 6)()
+        self._call("averages", self._ctx, out)
+        return tuple(out)
+
+    def reset_rows(self, which):
+        self._call("reset_rows", self._ctx, int(which))
+
+    def set_average_area(self, area):
+        self._call("set_average_area", self._ctx, float(area))
+
+    def assign_lattice(self, bubbles_per_dim, avg_rad, ux, uy, uz, uw, nr):
+        """init()'s lattice placement from the generator's draws; returns
+        (average initial area, largest radius)."""
+        import numpy as np
+        n = len(ux)
+        rows = [np.ascontiguousarray(a, dtype=np.float64) for a in (ux, uy, uz, uw, nr)]
+        bpd = _abi.I3(*[int(v) for v in bubbles_per_dim])
+        area, mr = C.c_double(), C.c_double()
+        ptr = [r.ctypes.data_as(_abi.PD) for r in rows]
+        self._call("assign_lattice", self._ctx, bpd, float(avg_rad), *ptr, int(n),
+                   C.byref(area), C.byref(mr))
+        return area.value, mr.value
+
 
 class _BatchFoam(GpuFoam):
     """A foam owned by a GpuFoamBatch (its context lives as long as the batch)."""

@@ -91,6 +91,9 @@ class Report(C.Structure):
         ("num_pairs", C.c_int32),
         ("status", C.c_int32),
         ("pad_", C.c_int32),
+        ("dt_min", C.c_double),
+        ("dt_max", C.c_double),
+        ("dt_sum", C.c_double),
     ]
 
     def as_dict(self):
@@ -102,6 +105,11 @@ ATTEMPT_D_ROWS = ["xp", "yp", "zp", "rp", "dxdtp", "dydtp", "dzdtp", "drdtp",
 ATTEMPT_SCALARS = ["total_area", "total_area_per_radius", "total_overlap_area",
                    "total_overlap_area_per_radius", "total_volume_new",
                    "max_error", "max_radius", "max_expansion"]
+
+
+class Stop(C.Structure):
+    _fields_ = [("time_integer", C.c_uint64), ("time_fraction", C.c_double),
+                ("max_radius", C.c_double), ("min_count", C.c_int32), ("pad_", C.c_int32)]
 
 
 class AttemptView(C.Structure):
@@ -143,6 +151,13 @@ def declare(lib, prefix):
             "profile_kernels": (C.c_int, [vp, C.c_int32, C.POINTER(C.c_double)]),
             "energy_noalloc": (C.c_int, [C.POINTER(Config), vp, vp, vp, vp, vp, vp,
                                          C.c_int32, C.c_int32, vp, vp]),
+            "integrate_until": (C.c_int, [vp, C.c_int64, C.POINTER(Stop), C.POINTER(Report)]),
+            "transform_positions": (C.c_int, [vp, C.c_int32]),
+            "averages": (C.c_int, [vp, C.POINTER(C.c_double)]),
+            "reset_rows": (C.c_int, [vp, C.c_int32]),
+            "set_average_area": (C.c_int, [vp, C.c_double]),
+            "assign_lattice": (C.c_int, [vp, I3, C.c_double, PD, PD, PD, PD, PD, C.c_int32,
+                                         C.POINTER(C.c_double), C.POINTER(C.c_double)]),
             "batch_create": (C.c_int, [C.POINTER(Config), C.c_int32, C.POINTER(vp)]),
             "batch_destroy": (C.c_int, [vp]),
             "batch_context": (C.c_int, [vp, C.c_int32, C.POINTER(vp)]),

@@ -52,8 +52,34 @@ def _compile(src, verbose):
     return obj, r.stderr
 
 
+CLI_SRC = os.path.join(HERE, "cli", "cubble_cli.cpp")
+CLI = os.path.join(HERE, "cubble-cli")
+
+
+def build_cli(force=False):
+    """Builds the cubble-cli executable (C++ over the C ABI, static cuRAND)
+    next to the library. Returns its path, or None with a message on stderr
+    when the toolchain lacks a part (the library does not depend on it)."""
+    deps = [CLI_SRC, os.path.join(HERE, "cli", "json.hpp"), LIB,
+            os.path.join(INCLUDE, "cubble_gb300.h")]
+    if not force and os.path.exists(CLI) and all(
+            os.path.getmtime(p) <= os.path.getmtime(CLI) for p in deps):
+        return CLI
+    tmp = CLI + ".tmp"
+    cmd = [nvcc()] + ARCH + ["-O2", "-std=c++17", "-Xcompiler", "-ffp-contract=off",
+                             "-I", INCLUDE, CLI_SRC, "-o", tmp, "-L" + HERE, "-lcubble_gb300",
+                             "-lcurand_static", "-lculibos", "-Xlinker", "-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        sys.stderr.write("cubble-cli not built:\n%s%s" % (r.stdout, r.stderr))
+        return None
+    os.replace(tmp, CLI)
+    return CLI
+
+
 def build(force=False, verbose=False):
     if not force and not _stale():
+        build_cli()
         return LIB
     os.makedirs(OUT, exist_ok=True)
     srcs = sources()
@@ -69,6 +95,7 @@ def build(force=False, verbose=False):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
     os.replace(tmp, LIB)
+    build_cli(force=True)
     return LIB
 
 

@@ -83,7 +83,8 @@ __global__ void __launch_bounds__(1024) k_batch_decide(const Bufs *bb, int count
                 const int accepted = !c->too_large;
                 if (ok && accepted && c->need_delete) sel |= SEL_DELETE;
                 if (ok && accepted && c->need_search) sel |= SEL_SEARCH;
-                if (ok && (c->too_large || c->steps < c->steps_target)) sel |= SEL_ATTEMPT;
+                if (ok && (c->too_large || (c->steps < c->steps_target && !c->stop_hit)))
+                    sel |= SEL_ATTEMPT;
             }
             c->bsel = sel;
             va = c->vgrid_a;

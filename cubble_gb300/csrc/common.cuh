@@ -112,6 +112,17 @@ struct Ctrl {
     // takes part in next (BatchSel bits, set between launches) and the
     // blocks of its virtual grid in the attempt and in the search / deletion.
     int bsel, vgrid_a, vgrid_s;
+    // Stop conditions of cb_integrate_until, checked after every accepted
+    // step (simulate()'s loop, src/simulator.cu:1002-1011 and the print and
+    // snapshot times of :1017-1029, :1090-1104): time >= (stop_tint,
+    // stop_tfrac), bubbles left <= stop_nmin, largest radius >= stop_rmax.
+    int stop_on, stop_hit;
+    int stop_nmin, pad_stop;
+    unsigned long long stop_tint;
+    double stop_tfrac, stop_rmax;
+    // Smallest, largest and summed dt after the accepted steps since the
+    // last reset (simulate()'s min / max / avg ts, src/simulator.cu:1013-1016).
+    double dt_min, dt_max, dt_sum;
     unsigned int done[DC_COUNT];
 };
 
@@ -413,18 +424,29 @@ __device__ void finish_attempt(Ctrl *c, const DevConst &k, double fErr, double f
         c->tfrac += c->dt;
         c->tint += (unsigned long long)c->tfrac;
         c->tfrac = c->tfrac - (double)(unsigned long long)c->tfrac;
+        c->dt_min = fmin(c->dt_min, c->dt);
+        c->dt_max = fmax(c->dt_max, c->dt);
+        c->dt_sum += c->dt;
         if (gas) {
             c->max_bubble_radius = fRad;
             c->need_delete = c->ndel > 0;
         }
         c->need_search = fExp >= 0.5 * k.skin;
+        if (c->stop_on) {
+            const int left = n - (c->need_delete ? c->ndel : 0);
+            const int time_up = c->tint > c->stop_tint ||
+                                (c->tint == c->stop_tint && c->tfrac >= c->stop_tfrac);
+            c->stop_hit = time_up || left <= c->stop_nmin ||
+                          (gas && c->max_bubble_radius >= c->stop_rmax);
+        }
     }
     if (c->graph_mode) {
         const int ok = c->status == CB_OK;
         const int accepted = !too_large;
         set_cond(c->h_delete, ok && accepted && c->need_delete);
         set_cond(c->h_search, ok && accepted && c->need_search);
-        set_cond(c->h_loop, ok && (too_large || c->steps < c->steps_target));
+        set_cond(c->h_loop,
+                 ok && (too_large || (c->steps < c->steps_target && !c->stop_hit)));
     }
 }
 

@@ -148,6 +148,7 @@ int integrate_eager(cb_context *c, int64_t n_steps) {
             rc = sync_status(c);
             if (rc) return rc;
         }
+        if (c->hctrl->stop_hit) break;
     }
     return sync_status(c);
 }
@@ -284,6 +285,9 @@ void fill_report(const cb_context *c, cb_report *r) {
     r->count = h.n;
     r->num_pairs = h.np;
     r->status = h.status;
+    r->dt_min = h.dt_min;
+    r->dt_max = h.dt_max;
+    r->dt_sum = h.dt_sum;
 }
 
 }  // namespace cbg
@@ -372,7 +376,7 @@ int cb_create(const cb_config *cfg, cb_context **out) {
     if ((rc = c->alloc(&b.moveDst, cap))) return bail(rc);
     if ((rc = c->alloc(&b.keep, pcap + 1))) return bail(rc);
     if ((rc = c->alloc(&b.keepScan, pcap + 1))) return bail(rc);
-    if ((rc = c->alloc(&b.energy, cap))) return bail(rc);
+    if ((rc = c->alloc(&b.energy, std::max<size_t>(cap, 8)))) return bail(rc);
     if (cudaMemcpyAsync(c->d_dslots, c->dslot, sizeof(c->dslot), cudaMemcpyHostToDevice,
                         c->stream) != cudaSuccess ||
         cudaMemcpyAsync(c->d_islots, c->islot, sizeof(c->islot), cudaMemcpyHostToDevice,
@@ -391,6 +395,9 @@ int cb_create(const cb_config *cfg, cb_context **out) {
     for (int r = 0; r < NI_ROLES; r++) h.irole[r] = r;
     for (int r = 0; r < NP_ROLES; r++) h.prole[r] = r;
     h.dt = cfg->time_step;
+    h.dt_min = 9999999.9;
+    h.dt_max = -1.0;
+    h.dt_sum = 0.0;
     h.use_gas = cfg->use_gas_exchange ? 1 : 0;
     h.use_flow = cfg->use_flow ? 1 : 0;
     h.inc_path = cfg->increment_path ? 1 : 0;
@@ -757,6 +764,28 @@ int cb_integrate_timed(cb_context *c, int64_t n_steps, cb_report *r, double *ms)
         fill_report(c, r);
     }
     return rc;
+}
+
+int cb_integrate_until(cb_context *c, int64_t max_steps, const cb_stop *stop, cb_report *r) {
+    CB_ENTER(c);
+    if (!stop) return fail(CB_ERR_INVALID_ARGUMENT, "null stop conditions");
+    int rc = c->pull();
+    if (rc) return rc;
+    Ctrl &h = *c->hctrl;
+    h.stop_on = 1;
+    h.stop_hit = 0;
+    h.stop_tint = stop->time_integer;
+    h.stop_tfrac = stop->time_fraction;
+    h.stop_nmin = stop->min_count;
+    h.stop_rmax = stop->max_radius;
+    if ((rc = c->push())) return rc;
+    rc = integrate_impl(c, max_steps);
+    int rc2 = c->pull();
+    h.stop_on = 0;
+    h.stop_hit = 0;
+    if (!rc2) rc2 = c->push();
+    if (r) fill_report(c, r);
+    return rc ? rc : rc2;
 }
 
 int cb_get_report(cb_context *c, cb_report *r) {

@@ -43,7 +43,7 @@ extern "C" {
 #define CB_ERR_STATE 8            /* call made in the wrong order             */
 
 #define CB_PRECISION_FP64 0  /* plain FP64 form (reference arithmetic)        */
-#define CB_PRECISION_MIXED 1 /* FP32 pair geometry on exact 32-bit fixed-point
+#define CB_PRECISION_MIXED 1 /* FP32 pair geometry on exact 64-bit fixed-point
                                 differences, FP64 positions/volume/error     */
 
 /* ------------------------------------------------------------ constants */
@@ -115,6 +115,9 @@ typedef struct cb_report {
     int32_t num_pairs;      /* pairs                                       */
     int32_t status;         /* CB_* status of the device control block     */
     int32_t pad_;
+    double dt_min;          /* smallest / largest / summed dt after the    */
+    double dt_max;          /* accepted steps since the last               */
+    double dt_sum;          /* cb_reset_rows(CB_RESET_DT_STATS)            */
 } cb_report;
 
 /* Outputs of one step() attempt (src/simulator.cu:192-249), before the
@@ -194,6 +197,63 @@ CB_API int cb_integrate(cb_context *ctx, int64_t n_steps, cb_report *report);
 CB_API int cb_integrate_timed(cb_context *ctx, int64_t n_steps, cb_report *report,
                        double *device_ms);
 CB_API int cb_get_report(cb_context *ctx, cb_report *report);
+
+/* Conditions that end cb_integrate_until after an accepted step: the
+ * simulate() loop's stop test (src/simulator.cu:1002-1011: bubbles left
+ * <= min_count, or the largest radius >= max_radius, the latter only with
+ * gas exchange) and its print / snapshot times (:1017-1029, :1090-1104:
+ * time >= time_integer + time_fraction). */
+typedef struct cb_stop {
+    uint64_t time_integer;
+    double time_fraction;
+    double max_radius;
+    int32_t min_count;
+    int32_t pad_;
+} cb_stop;
+
+/* Up to max_steps accepted steps (integrate() calls), ending after the
+ * first step that meets a condition of *stop; checked on the device, so a
+ * graph context runs the whole stretch as one graph launch. The caller
+ * reads which condition held from the report (time, count, max_radius). */
+CB_API int cb_integrate_until(cb_context *ctx, int64_t max_steps, const cb_stop *stop,
+                              cb_report *report);
+
+/* transformPositions (src/kernels.cu:971-990): normalize != 0 maps the
+ * positions to [0, 1] of the current box, 0 maps them back from [0, 1]
+ * into the box; init()'s box rescale (src/simulator.cu:793-833) is
+ * transform(1), cb_set_box(new box), transform(0). */
+CB_API int cb_transform_positions(cb_context *ctx, int32_t normalize);
+
+/* Means over the bubbles of r, dxdt, dydt, dzdt, drdt and path
+ * (simulate()'s getAvg, src/simulator.cu:1038-1052), in that order. */
+CB_API int cb_averages(cb_context *ctx, double means[6]);
+
+/* Resets of simulate() and init(): CB_RESET_ERROR zeroes the error row
+ * (resetArrays after each print, src/simulator.cu:1106-1110, and at the end
+ * of init, :947-948), CB_RESET_WRAP the wrap counts (:941-945),
+ * CB_RESET_DT_STATS the dt statistics of the report. */
+#define CB_RESET_ERROR 1
+#define CB_RESET_WRAP 2
+#define CB_RESET_DT_STATS 4
+CB_API int cb_reset_rows(cb_context *ctx, int32_t which);
+
+/* averageSurfaceAreaIn (init() computes it from the initial radii,
+ * src/simulator.cu:697-703; the mean-field gas exchange uses it). */
+CB_API int cb_set_average_area(cb_context *ctx, double average_surface_area_in);
+
+/* The initial foam of init() (src/simulator.cu:676-711): from the draws of
+ * the reference's generator (uniform x, y, z and w, normal r; host rows of
+ * `count` doubles, z ignored in 2D) and bubbles_per_dim, places bubble i on
+ * its lattice point plus a random offset, fixes its radius
+ * (assignDataToBubbles, src/kernels.cu:1026-1071) and loads the result as
+ * the state (index = i, rates and path zero). *avg_area receives the mean
+ * initial area (averageSurfaceAreaIn), *max_radius the largest radius. The
+ * box of the context must be the lattice box: lbb and tfr = lbb +
+ * 2 avg_rad bubbles_per_dim. */
+CB_API int cb_assign_lattice(cb_context *ctx, const int32_t bubbles_per_dim[3], double avg_rad,
+                             const double *ux, const double *uy, const double *uz,
+                             const double *uw, const double *nr, int32_t count,
+                             double *avg_area, double *max_radius);
 
 /* totalEnergy() (src/simulator.cu:39-58, kernel src/kernels.cu:941-957). */
 CB_API int cb_energy(cb_context *ctx, double *energy);

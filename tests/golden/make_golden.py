@@ -19,6 +19,8 @@ records, for small seeded foams:
            integrate() and removeBubbles() (swapDataCountPairs,
            addVolumeFixPairs) with the deletion list in ascending order;
   energy   potentialEnergy (src/kernels.cu:941-957).
+With --init it writes init_2d.npz / init_3d.npz instead: init()'s
+assignDataToBubbles on seeded draws and transformPositions both ways.
 
 Run on the GPU machine (torch provides the device buffers, ctypes the driver API):
     python tests/golden/make_golden.py [out_dir]
@@ -392,6 +394,58 @@ def ref_energy(drv, cfg, st, pi, pj):
     return f.tempD1[:n].cpu().numpy()
 
 
+def ref_init(drv, dim, seed):
+    """assignDataToBubbles (src/kernels.cu:1026-1071) on seeded uniform and
+    normal draws for a lattice box, then transformPositions
+    (src/kernels.cu:971-990) to [0, 1] and back into a rescaled box."""
+    from cubble_gb300 import workloads
+    rng = np.random.default_rng(seed)
+    bpd = (23, 19, 7 if dim == 3 else 1)
+    n = bpd[0] * bpd[1] * bpd[2]
+    avg_rad = 1.0
+    side = [2.0 * avg_rad * bpd[a] if a < dim else 0.0 for a in range(3)]
+    cfg, _ = workloads.foam(4, dim, 0.9, seed=1)
+    cfg.lbb[0] = cfg.lbb[1] = cfg.lbb[2] = 0.0
+    for a in range(3):
+        cfg.tfr[a] = side[a]
+    cfg.min_rad = 0.1 * avg_rad
+    data = {"bpd": np.array(bpd, np.int32), "avg_rad": np.array(avg_rad),
+            "lbb": np.zeros(3), "tfr": np.array(side), "min_rad": np.array(cfg.min_rad)}
+    draws = {"ux": rng.random(n), "uy": rng.random(n), "uz": rng.random(n) * (dim == 3),
+             "uw": rng.random(n), "nr": rng.normal(avg_rad, 0.21, n)}
+    draws["nr"][:5] = [-0.4, 0.05, -0.02, 0.0999, 0.1001]  # negative and small radii
+    data.update({"in_" + k: v for k, v in draws.items()})
+    f = Foam(drv, cfg, n, 64)
+    f.put("x", draws["ux"])
+    f.put("y", draws["uy"])
+    f.put("z", draws["uz"])
+    f.put("rp", draws["uw"])
+    f.put("r", draws["nr"])
+    drv.launch("assignDataToBubbles", [IVec(*bpd), C.c_double(avg_rad), f.bubbles()])
+    drv.sync()
+    for k in ("x", "y", "z", "r", "rp", "index"):
+        data["out_" + k] = f.get(k)
+    # box rescale: to [0, 1], new box, back (src/simulator.cu:793-833)
+    drv.launch("transformPositions", [C.c_bool(True), f.bubbles()])
+    drv.sync()
+    for k in ("x", "y", "z"):
+        data["norm_" + k] = f.get(k)
+    new_tfr = [0.9 * side[0], 1.1 * side[1], 0.95 * side[2] if dim == 3 else 0.0]
+    cfg2, _ = workloads.foam(4, dim, 0.9, seed=1)
+    for a in range(3):
+        cfg2.lbb[a] = 0.0
+        cfg2.tfr[a] = new_tfr[a]
+    g = Foam(drv, cfg2, n, 64)
+    for k in ("x", "y", "z"):
+        g.put(k, data["norm_" + k])
+    drv.launch("transformPositions", [C.c_bool(False), g.bubbles()])
+    drv.sync()
+    data["new_tfr"] = np.array(new_tfr)
+    for k in ("x", "y", "z"):
+        data["back_" + k] = g.get(k)
+    return data
+
+
 # ------------------------------------------------------------------ cases
 def cases():
     from cubble_gb300 import workloads
@@ -484,5 +538,19 @@ def main(out_dir):
         print("wrote", path, "pairs", len(pairs), "deleted", len(res["to_be_deleted"]))
 
 
+def main_init(out_dir):
+    os.makedirs(out_dir, exist_ok=True)
+    drv = Driver(CUBIN)
+    for dim in (2, 3):
+        path = os.path.join(out_dir, "init_%dd.npz" % dim)
+        np.savez_compressed(path, **ref_init(drv, dim, 600 + dim))
+        print("wrote", path)
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "gpurun_out", "golden"))
+    args = [a for a in sys.argv[1:] if a != "--init"]
+    out = args[0] if args else os.path.join(ROOT, "gpurun_out", "golden")
+    if "--init" in sys.argv:
+        main_init(out)
+    else:
+        main(out)
