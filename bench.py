@@ -41,9 +41,62 @@ def workload(name, seed, precision=0, use_graph=1):
     elif name == "c1":
         cfg, st = workloads.config_c1(seed=seed, precision=precision, use_graph=use_graph)
         desc = "2D periodic foam N=1e4, phi=0.90, r~N(1,0.1) in [0.3,2.0], kappa=0.01, K=0.1, tol 1e-5"
+    elif name.startswith("c5"):
+        # "c5" is N=1e7; "c5:<n>" the same foam at another size
+        n = int(float(name.split(":")[1])) if ":" in name else 10_000_000
+        cfg, st = workloads.config_c5(seed=seed, n=n, precision=1, use_graph=use_graph)
+        desc = ("3D foam N=%d, walls in z, periodic x/y, linear shear along x (max speed "
+                "0.05), phi=0.80, r~N(1,0.15) in [0.3,2.5], kappa=0.01, K=0.1, tol 1e-5, "
+                "mixed" % n)
     else:
         raise SystemExit("unknown workload " + name)
     return cfg, st, desc
+
+
+def run_until_deleted(args):
+    """The large sheared foam run until a fraction of its bubbles is gone:
+    device time, bubble-steps/s over the whole run (searches and every
+    compaction included), the device memory it holds, progress samples."""
+    import torch
+    import cubble_gb300 as cb
+    from cubble_gb300 import workloads
+    torch.cuda.set_device(0)
+    cb.build()
+    cfg, st, desc = workload(args.workload, args.seed, precision=1, use_graph=1)
+    n0 = len(st["x"])
+    free0, total = torch.cuda.mem_get_info()
+    sim = cb.GpuFoam(cfg)
+    sim.load_state(st)
+    free1, _ = torch.cuda.mem_get_info()
+    workloads.prepare(sim)
+    target = int(n0 * (1.0 - args.until_deleted))
+    r0 = sim.report()
+    samples, dev_ms = [], 0.0
+    t0 = time.perf_counter()
+    r = r0
+    while r["count"] > target and r["steps"] - r0["steps"] < args.max_run_steps:
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        r = sim.integrate_until(args.chunk_steps, min_count=target)
+        ev1.record()
+        torch.cuda.synchronize()
+        dev_ms += ev0.elapsed_time(ev1)
+        samples.append({"steps": r["steps"] - r0["steps"], "count": r["count"],
+                        "searches": r["searches"] - r0["searches"],
+                        "time": r["time_integer"] + r["time_fraction"],
+                        "wall_s": time.perf_counter() - t0})
+    bs = r["bubble_steps"] - r0["bubble_steps"]
+    line = {"metric": "bubble-steps/s, large sheared foam run to %.0f%% deleted"
+                      % (100 * args.until_deleted),
+            "value": bs / (dev_ms / 1e3), "unit": "bubble-steps/s", "workload": desc,
+            "bubbles_start": n0, "bubbles_end": r["count"],
+            "reached_target": r["count"] <= target,
+            "steps": r["steps"] - r0["steps"], "attempts": r["attempts"] - r0["attempts"],
+            "searches": r["searches"] - r0["searches"], "deleted": r["deleted"] - r0["deleted"],
+            "device_s": dev_ms / 1e3, "device_bytes_held": int(free0 - free1),
+            "device_total_bytes": int(total), "samples": samples[-20:]}
+    sim.close()
+    print(json.dumps(line))
 
 
 def peaks():
@@ -583,6 +636,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--until-deleted", type=float, default=0.0)
+    ap.add_argument("--chunk-steps", type=int, default=2000)
+    ap.add_argument("--max-run-steps", type=int, default=200000)
     ap.add_argument("--batch-count", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=300)
     ap.add_argument("--batch-tune-steps", type=int, default=10)
@@ -593,11 +649,11 @@ def main():
         world = int(os.environ.get("WORLD_SIZE", "1"))
         run_reference(args, world, int(os.environ.get("RANK", "0")))
         return
+    if args.until_deleted > 0.0:
+        run_until_deleted(args)
+        return
     world, rank, local = dist_setup()
-    if False:
-        pass
-    else:
-        run_gb300(args, world, rank, local)
+    run_gb300(args, world, rank, local)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

@@ -58,6 +58,7 @@ class Config(C.Structure):
         ("average_surface_area_in", C.c_double),
         ("error_tolerance", C.c_double),
         ("time_step", C.c_double),
+        ("shear_speed", C.c_double),
     ]
 
 

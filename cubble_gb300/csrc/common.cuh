@@ -75,6 +75,11 @@ struct DevConst {
     float pre_margin;  // FP32 pair-search prefilter margin (length units)
     float half_iv32[3];
     float iv32[3];
+    // Linear shear flow (cb_config.shear_speed): v_x += shear (2 (q - lbb_q)
+    // / L_q - 1) on the last axis q; shear_il = 2 / L_q.
+    int shear_on, shear_axis;
+    double shear, shear_il;
+    float shear_f, shear_il_f;
 };
 
 // Device control block. The host reads it after each eager phase or at the

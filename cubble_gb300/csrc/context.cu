@@ -87,6 +87,12 @@ void fill_const(cb_context *c) {
     // FP32 coordinates carry |x| 2^-24 rounding; 1e-5 (maxabs + interval) is
     // more than 20x the worst error of the prefiltered distance.
     k.pre_margin = (float)(1e-5 * (maxabs + maxiv) + 1e-4);
+    k.shear_on = f.shear_speed != 0.0 ? 1 : 0;
+    k.shear_axis = k.dim - 1;
+    k.shear = f.shear_speed;
+    k.shear_il = k.iv[k.shear_axis] > 0.0 ? 2.0 / k.iv[k.shear_axis] : 0.0;
+    k.shear_f = (float)k.shear;
+    k.shear_il_f = (float)k.shear_il;
 }
 
 }  // namespace

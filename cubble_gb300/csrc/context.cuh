@@ -76,7 +76,11 @@ struct cb_context {
         CB_CUDA(cudaStreamSynchronize(stream));
         return CB_OK;
     }
-    int mode() const { return (hctrl->use_gas ? 1 : 0) | (hctrl->use_flow ? 2 : 0); }
+    // kernel variant: bit 1 gas exchange, bit 2 the box-region flow (its
+    // neighbour sums); the shear flow needs no pair work
+    int mode() const {
+        return (hctrl->use_gas ? 1 : 0) | (hctrl->use_flow && !hk.shear_on ? 2 : 0);
+    }
     int check_launch() {
         CB_CUDA(cudaGetLastError());
         return CB_OK;

@@ -226,7 +226,8 @@ __device__ __forceinline__ void k_correct_body(const Bufs &b, const int vb, cons
     const int n = c->n;
     const double ts = c->dt;
     const double h = 0.5 * ts;
-    const int gas = c->use_gas, flow = c->use_flow, path = c->inc_path;
+    const int gas = c->use_gas, path = c->inc_path;
+    const int flow = c->use_flow && !k.shear_on, shear = c->use_flow && k.shear_on;
     const double *X = drow(b, c, RX), *Y = drow(b, c, RY), *Z = drow(b, c, RZ),
                  *R = drow(b, c, RR);
     double *XN = drow(b, c, RXN), *YN = drow(b, c, RYN), *ZN = drow(b, c, RZN),
@@ -276,6 +277,10 @@ __device__ __forceinline__ void k_correct_body(const Bufs &b, const int vb, cons
             }
             vpx += !inside * multiplier * a1.y + k.flow_vel[0] * inside;
             vpy += !inside * multiplier * a1.z + k.flow_vel[1] * inside;
+        }
+        if (shear) {  // linear shear along x over the last axis (cb_config.shear_speed)
+            const double q = DIM == 3 ? zp : yp;
+            vpx += k.shear * ((q - k.lbb[DIM - 1]) * k.shear_il - 1.0);
         }
         if (k.any_wall) {  // addWallVelocity, src/kernels.cu:546-593
             double xDrag = 1.0, yDrag = 1.0, velocity = 0.0;

@@ -445,6 +445,7 @@ __device__ __forceinline__ void k_correct_mx_body(const Bufs &b, const int vb, c
     const float mfa = float_from_double(c->mfa), mfb = float_from_double(c->mfb);
     const float kq = k.kq_f;
     const long long minr = __double_as_longlong(k.min_rad);
+    const bool shear = c->use_flow && k.shear_on;
     long long merr = 0, mrad = 0;
     float mexp = 0.f;
     double vol = 0.0;
@@ -464,7 +465,7 @@ __device__ __forceinline__ void k_correct_mx_body(const Bufs &b, const int vb, c
             or_ = CB_F(RVO3)[i];
             rp = fmaf(h, fmaf(3.f, vr, -or_), rp);  // as k_predict_mx
         }
-        if (FLOW || WALLS) {
+        if (FLOW || WALLS || shear) {
             // predicted coordinates as x0 + e (e the FP32 AB2 increment)
             const float ex = h * fmaf(3.f, vx, -ox), ey = h * fmaf(3.f, vy, -oy),
                         ez = h * fmaf(3.f, vz, -oz);
@@ -488,6 +489,11 @@ __device__ __forceinline__ void k_correct_mx_body(const Bufs &b, const int vb, c
                 }
                 vpx += !inside * multiplier * fl.x + (float)k.flow_vel[0] * inside;
                 vpy += !inside * multiplier * fl.y + (float)k.flow_vel[1] * inside;
+            }
+            if (shear) {  // linear shear along x over the last axis (cb_config.shear_speed)
+                const float q = DIM == 3 ? float_from_double(z0 - k.lbb[2]) + ez
+                                         : float_from_double(y0 - k.lbb[1]) + ey;
+                vpx += k.shear_f * fmaf(q, k.shear_il_f, -1.f);
             }
             if (WALLS) {  // addWallVelocity, src/kernels.cu:546-593
                 const float drag = (float)(1.0 - k.wall_drag);

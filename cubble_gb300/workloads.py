@@ -69,6 +69,15 @@ def config_c2(seed=2, n=1_000_000, **kw):
                 kappa=0.01, k_param=0.1, **kw)
 
 
+def config_c5(seed=5, n=10_000_000, precision=1, **kw):
+    """3D, walls in z (drag 0.1), periodic x / y, linear shear along x with
+    maximum speed 0.05 at the walls, N=1e7, phi=0.80, r~N(1,0.15) in
+    [0.3,2.5], kappa=0.01, K=0.1, tol 1e-5, mixed precision."""
+    return foam(n, 3, 0.80, 1.0, 0.15, (0.3, 2.5), seed=seed, kappa=0.01, k_param=0.1,
+                wall=(0, 0, 1), wall_drag=0.1, use_flow=1, shear_speed=0.05,
+                precision=precision, **kw)
+
+
 def prepare(sim):
     """Initial neighbour search and the Euler bootstrap of the AB2 history,
     the part of init() between the first search and stabilisation

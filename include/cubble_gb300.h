@@ -79,6 +79,13 @@ typedef struct cb_config {
     double average_surface_area_in;  /* <A_in>                             */
     double error_tolerance;  /* HostData.errorTolerance                    */
     double time_step;        /* initial dt (HostData.timeStep)             */
+    /* Extension, not in the reference: with use_flow and shear_speed != 0
+     * the imposed flow is a linear shear instead of addFlowVelocity's box
+     * region: every bubble's velocity gains shear_speed * (2 (q - lbb_q) /
+     * L_q - 1) along x, q its predicted coordinate on the last axis (z in
+     * 3D, y in 2D): -shear_speed at the lower wall, +shear_speed at the
+     * upper one. */
+    double shear_speed;
 } cb_config;
 
 /* Host view of the persistent per-bubble state, keyed by the bubble order of

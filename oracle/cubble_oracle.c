@@ -842,6 +842,15 @@ static void add_flow_velocity(cbo_ctx *c, int i) {
     c->vp[1][i] += !inside * multiplier * c->fv[1][i] + fvel[1] * inside;
 }
 
+/* Linear shear along x over the last axis (cb_config.shear_speed, an
+ * extension of this library; the reference has only the box-region flow). */
+static void add_shear_velocity(cbo_ctx *c, int i) {
+    const int q = c->dim - 1;
+    const double len = c->tfr[q] - c->lbb[q];
+    const double pos = c->xp[q][i];
+    c->vp[0][i] += c->cfg.shear_speed * ((pos - c->lbb[q]) * (2.0 / len) - 1.0);
+}
+
 /* touchesWall lambda of addWallVelocity, src/kernels.cu:553-566 */
 static inline int touches_wall(double f0, double rad, double x, double low,
                                double high, double *velocity) {
@@ -906,6 +915,7 @@ static void post_integrate(cbo_ctx *c, double ts) {
     const int n = c->n, dim = c->dim, gas = c->use_gas, flow = c->use_flow,
               path = c->inc_path;
     const int walls = c->cfg.wall[0] || c->cfg.wall[1] || c->cfg.wall[2];
+    const int shear = c->cfg.shear_speed != 0.0;
     double *vol = c->tmpd;
     double merr = 0.0, mrad = 0.0, mexp = 0.0;
     int nonfinite = 0;
@@ -916,7 +926,8 @@ static void post_integrate(cbo_ctx *c, double ts) {
 #pragma omp parallel for num_threads(c->nthreads) schedule(static) reduction(max : merr, mrad, mexp) reduction(| : nonfinite)
 #endif
     for (int i = 0; i < n; i++) {
-        if (flow) add_flow_velocity(c, i);
+        if (flow && !shear) add_flow_velocity(c, i);
+        if (flow && shear) add_shear_velocity(c, i);
         if (walls) add_wall_velocity(c, i);
         double e = 0.0, temp = 0.0, dist = 0.0;
         temp = correct1(ts, c->xp[0], c->x[0], c->v[0], c->vp[0], c->saved[0], i, &e);
@@ -984,7 +995,7 @@ static int step_once(cbo_ctx *c) {
     const double ts = c->dt;
     c->attempts++;
     pre_integrate(c, ts);
-    pairwise(c, c->use_gas, c->use_flow);
+    pairwise(c, c->use_gas, c->use_flow && c->cfg.shear_speed == 0.0);
     post_integrate(c, ts);
     const double tol = c->cfg.error_tolerance;
     const int too_large = c->max_err > tol;

@@ -100,6 +100,36 @@ def test_flow_attempt(oracle_mod):
     assert_rows_close(ag, ao, ["xp", "yp", "dxdtp", "dydtp", "drdtp"], 1e-11, "flow ")
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_shear_attempt_and_trajectory(oracle_mod, precision):
+    """The linear shear extension (walls in z, shear along x) against the
+    oracle's restatement: FP64 within 1e-11, the mixed form within 1e-6."""
+    cfg, st = make("3d-wallz", use_flow=1, shear_speed=0.05)
+    cfg_g, _ = make("3d-wallz", use_flow=1, shear_speed=0.05, precision=precision)
+    g = cb.GpuFoam(cfg_g)
+    o = oracle_mod.OracleFoam(cfg)
+    for f in (g, o):
+        f.load_state(st)
+        workloads.prepare(f)
+        f.integrate(3)
+    if precision:
+        i, j = o.pairs()
+        g.load_state(o.get_state())
+        g.set_pairs(i, j)
+        g.set_time(o.report()["time_step"])
+    ag, ao = g.attempt(), o.attempt()
+    tol = 1e-6 if precision else 1e-11
+    assert_rows_close(ag, ao, ["dxdtp", "dydtp", "dzdtp", "drdtp"], tol, "shear ")
+    # the imposed profile: mean x velocity grows with height
+    s = o.get_state()
+    z, vx = s["z"], ao["dxdtp"]
+    lo, hi = z < np.quantile(z, 0.2), z > np.quantile(z, 0.8)
+    assert vx[hi].mean() - vx[lo].mean() > 0.02
+    rg, ro = g.integrate(10), o.integrate(10)
+    for k in ("steps", "searches", "deleted", "count"):
+        assert rg[k] == ro[k], k
+
+
 @pytest.mark.parametrize("graph", [0, 1])
 @pytest.mark.parametrize("case", ["2d", "3d", "3d-wallz"])
 def test_trajectory(oracle_mod, case, graph):

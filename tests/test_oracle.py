@@ -238,3 +238,25 @@ def test_energy_and_volume(oracle_mod):
     e = np.where(e > 0, e * e, 0.0)
     assert f.energy() == pytest.approx(2 * e.sum(), rel=1e-12)
     assert f.total_volume() == pytest.approx(float(np.sum(4 / 3 * math.pi * s["r"] ** 3)), rel=1e-12)
+
+
+def test_oracle_shear_profile():
+    """Linear shear (extension): an isolated bubble at height q gains
+    shear_speed * (2 (q - lbb) / L - 1) along x and nothing else."""
+    from cubble_gb300 import workloads
+    from oracle.oracle import OracleFoam
+    cfg, _ = workloads.foam(4, 3, 0.5, seed=3, wall=(0, 0, 1), use_flow=1,
+                            shear_speed=0.05)
+    L = 40.0
+    for a in range(3):
+        cfg.tfr[a] = L
+    st = {"x": np.array([5.0, 15.0, 25.0, 35.0]), "y": np.full(4, 20.0),
+          "z": np.array([10.0, 20.0, 30.0, 5.0]), "r": np.full(4, 1.0)}
+    o = OracleFoam(cfg)
+    o.load_state(st)
+    o.search_neighbors()
+    z = o.get_state()["z"]  # cell order after the search
+    a = o.attempt()
+    expect = 0.05 * (2.0 * z / L - 1.0)
+    np.testing.assert_allclose(a["dxdtp"], expect, rtol=1e-12, atol=1e-15)
+    np.testing.assert_allclose(a["dydtp"], 0.0, atol=1e-15)
