@@ -335,7 +335,9 @@ def measure_form(args, world, rank, precision, clocks_on=True):
     n_now = r1["count"]
     hbm, src = peaks()
     achieved = ab[names[top]] * n_now / (kms[top] * 1e-3) / 1e9
-    step_gbs = ab["step"] * n_now / (sum(kms) * 1e-3) / 1e9
+    # the whole step (searches, rejects, deletions and the skipped predict
+    # of a speculated prediction included): algorithmic bytes x measured rate
+    step_gbs = ab["step"] * (bs_all / el) / 1e9
     gas, flow = int(cfg.use_gas_exchange), int(cfg.use_flow)
     sfx = "_mx" if precision else ""
     walls = int(any(cfg.wall[:dim]))

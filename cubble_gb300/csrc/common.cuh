@@ -28,6 +28,9 @@ constexpr double kPi = 3.1415926535897932384626433832795028841971693993;
 constexpr int kBlock = 256;  // threads per block of every grid-stride kernel
 constexpr int kAcc = 8;      // FP64 accumulators per bubble
 constexpr int kPartSlots = 8;
+// Partners j > i per bubble the search's counting pass keeps (a bubble with
+// more sends the search through its second enumeration pass).
+__host__ __device__ constexpr int kStash(int dim) { return dim == 3 ? 32 : 16; }
 
 // Double-row roles (slot table indices are in Ctrl::drole).
 enum DRole : int {
@@ -117,6 +120,13 @@ struct Ctrl {
     // takes part in next (BatchSel bits, set between launches) and the
     // blocks of its virtual grid in the attempt and in the search / deletion.
     int bsel, vgrid_a, vgrid_s;
+    int stash_over;  // a row of the last search exceeded kStash partners
+    // Mixed form: the correct kernel also writes the next attempt's
+    // prediction for both dt it can have after an accept (unchanged, x1.269)
+    // with their area sums; pred_ready says the prediction for the coming
+    // attempt is in slot pred_slot (0 = pred, 1 / 2 = the candidates).
+    int pred_ready, pred_slot;
+    double cand_sumA[2], cand_sumAr[2];
     // Stop conditions of cb_integrate_until, checked after every accepted
     // step (simulate()'s loop, src/simulator.cu:1002-1011 and the print and
     // snapshot times of :1017-1029, :1090-1104): time >= (stop_tint,
@@ -139,6 +149,7 @@ struct Bufs {
     int *const *is;     // int slots
     int *const *ps;     // pair slots
     double *pred;       // 4 doubles per bubble
+    double *predc;      // mixed form: two candidate predictions, 8 doubles per bubble
     double *invr;       // 1 / rp (3D)
     double *acc;        // kAcc doubles per bubble
     double *part;       // kPartSlots x grid partials
@@ -159,6 +170,7 @@ struct Bufs {
     int *moveDst;       // cap
     int *keep;          // pcap + 1
     int *keepScan;      // pcap + 1
+    int *stash;         // cap x kStash(dim): pair partners found by the counting pass
     double *dbg_ov;     // optional copy of the overlap row (cb_attempt)
     double *energy;     // per-bubble energies
 };
@@ -301,8 +313,31 @@ __device__ __forceinline__ double rsqrt_hn(double a) {
     const double e = fma(-t, y, 1.0);
     return fma(y * e, fma(e, 0.375, 0.5), y);
 }
+// Sign and ordering on the integer pipe (no FP64 instruction): negation and
+// absolute value flip / clear the sign bit of the high word; for doubles
+// >= 0 (and +0) the signed 64-bit patterns order like the values.
+__device__ __forceinline__ double neg_bits(double x) {
+    int hi;
+    asm("xor.b32 %0, %1, 0x80000000;" : "=r"(hi) : "r"(__double2hiint(x)));
+    return __hiloint2double(hi, __double2loint(x));
+}
+__device__ __forceinline__ double abs_bits(double x) {
+    int hi;
+    asm("and.b32 %0, %1, 0x7fffffff;" : "=r"(hi) : "r"(__double2hiint(x)));
+    return __hiloint2double(hi, __double2loint(x));
+}
+__device__ __forceinline__ bool nonneg_bits(double x) { return __double2hiint(x) >= 0; }
+__device__ __forceinline__ bool less_nonneg(double a, double b) {
+    return __double_as_longlong(a) < __double_as_longlong(b);
+}
+__device__ __forceinline__ double min_nonneg(double a, double b) {
+    return __longlong_as_double(min(__double_as_longlong(a), __double_as_longlong(b)));
+}
+
 // sqrt(a) = a / sqrt(a) for a > 0, 0 for a <= 0.
-__device__ __forceinline__ double sqrt_hn(double a) { return a > 0.0 ? a * rsqrt_hn(a) : 0.0; }
+__device__ __forceinline__ double sqrt_hn(double a) {
+    return __double_as_longlong(a) > 0 ? a * rsqrt_hn(a) : 0.0;
+}
 
 // Minimum image on a periodic axis: |d| > L/2 is tested on the bit patterns
 // (non-negative doubles order like their bits), so the test costs no FP64
@@ -398,6 +433,16 @@ __device__ void finish_attempt(Ctrl *c, const DevConst &k, double fErr, double f
     else if (increase)
         c->dt *= 1.269;
     c->too_large = too_large;
+    if (k.mixed) {  // speculative prediction of the next attempt (step_mixed.cu)
+        const int use = !too_large && !c->no_accept;
+        c->pred_ready = use;
+        c->pred_slot = use ? (increase ? 2 : 1) : 0;
+        if (use) {
+            c->sumA = c->cand_sumA[increase ? 1 : 0];
+            c->sumAr = c->cand_sumAr[increase ? 1 : 0];
+        }
+        c->cand_sumA[0] = c->cand_sumA[1] = c->cand_sumAr[0] = c->cand_sumAr[1] = 0.0;
+    }
     if (fBad > 0.0 || isnan(fErr)) c->status = CB_ERR_NONFINITE;
     c->need_delete = 0;
     c->need_search = 0;

@@ -105,6 +105,16 @@ int sync_status(cb_context *c) {
     return CB_OK;
 }
 
+// A state change from the host (new rows, pairs, dt, options, box) makes
+// the candidate predictions of the mixed form stale.
+int invalidate_prediction(cb_context *c) {
+    int rc = c->pull();
+    if (rc) return rc;
+    c->hctrl->pred_ready = 0;
+    c->hctrl->pred_slot = 0;
+    return c->push();
+}
+
 // The three kernels of one step() attempt, in the context's precision.
 void launch_attempt_kernels(const cb_context *c, const Launch &l, const Bufs &b, int which) {
     const int dim = c->hk.dim;
@@ -362,6 +372,7 @@ int cb_create(const cb_config *cfg, cb_context **out) {
     if ((rc = c->alloc(&c->d_islots, NI_ROLES))) return bail(rc);
     if ((rc = c->alloc(&c->d_pslots, NP_ROLES))) return bail(rc);
     if ((rc = c->alloc(&b.pred, 4 * cap))) return bail(rc);
+    if (c->hk.mixed && (rc = c->alloc(&b.predc, 8 * cap))) return bail(rc);
     if ((rc = c->alloc(&b.invr, cap))) return bail(rc);
     if ((rc = c->alloc(&b.acc, (size_t)kAcc * cap))) return bail(rc);
     if ((rc = c->alloc(&b.part, (size_t)kPartSlots * G))) return bail(rc);
@@ -382,6 +393,7 @@ int cb_create(const cb_config *cfg, cb_context **out) {
     if ((rc = c->alloc(&b.moveDst, cap))) return bail(rc);
     if ((rc = c->alloc(&b.keep, pcap + 1))) return bail(rc);
     if ((rc = c->alloc(&b.keepScan, pcap + 1))) return bail(rc);
+    if ((rc = c->alloc(&b.stash, cap * (size_t)kStash(c->hk.dim)))) return bail(rc);
     if ((rc = c->alloc(&b.energy, std::max<size_t>(cap, 8)))) return bail(rc);
     if (cudaMemcpyAsync(c->d_dslots, c->dslot, sizeof(c->dslot), cudaMemcpyHostToDevice,
                         c->stream) != cudaSuccess ||
@@ -503,6 +515,8 @@ int cb_load_state(cb_context *c, const cb_state_view *s) {
     h.status = CB_OK;
     h.max_bubble_radius = mr;
     h.too_large = h.need_search = h.need_delete = h.attempts_this_step = 0;
+    h.pred_ready = 0;
+    h.pred_slot = 0;
     rc = c->push();  // synchronises, so the caller's buffers are free
     if (rc) return rc;
     c->loaded = true;
@@ -565,6 +579,12 @@ int cb_get_state(cb_context *c, cb_state_view *s) {
 }
 
 int cb_set_options(cb_context *c, int32_t g, int32_t f, int32_t p) {
+    {
+        if (!c) return fail(CB_ERR_INVALID_ARGUMENT, "null context");
+        CB_CUDA(cudaSetDevice(c->dev));
+        const int rc0 = invalidate_prediction(c);
+        if (rc0) return rc0;
+    }
     CB_ENTER(c);
     int rc = c->pull();
     if (rc) return rc;
@@ -575,6 +595,12 @@ int cb_set_options(cb_context *c, int32_t g, int32_t f, int32_t p) {
 }
 
 int cb_set_time(cb_context *c, double dt, uint64_t ti, double tf) {
+    {
+        if (!c) return fail(CB_ERR_INVALID_ARGUMENT, "null context");
+        CB_CUDA(cudaSetDevice(c->dev));
+        const int rc0 = invalidate_prediction(c);
+        if (rc0) return rc0;
+    }
     CB_ENTER(c);
     int rc = c->pull();
     if (rc) return rc;
@@ -586,6 +612,12 @@ int cb_set_time(cb_context *c, double dt, uint64_t ti, double tf) {
 
 int cb_set_box(cb_context *c, const double lbb[3], const double tfr[3], double m,
                const double flbb[3], const double ftfr[3]) {
+    {
+        if (!c) return fail(CB_ERR_INVALID_ARGUMENT, "null context");
+        CB_CUDA(cudaSetDevice(c->dev));
+        const int rc0 = invalidate_prediction(c);
+        if (rc0) return rc0;
+    }
     CB_ENTER(c);
     if (!lbb || !tfr) return fail(CB_ERR_INVALID_ARGUMENT, "null box");
     for (int a = 0; a < 3; a++) {
@@ -600,6 +632,12 @@ int cb_set_box(cb_context *c, const double lbb[3], const double tfr[3], double m
 }
 
 int cb_bootstrap(cb_context *c) {
+    {
+        if (!c) return fail(CB_ERR_INVALID_ARGUMENT, "null context");
+        CB_CUDA(cudaSetDevice(c->dev));
+        const int rc0 = invalidate_prediction(c);
+        if (rc0) return rc0;
+    }
     CB_ENTER(c);
     if (!c->loaded) return fail(CB_ERR_STATE, "state not loaded");
     const int dim = c->hk.dim;
@@ -649,6 +687,12 @@ int cb_get_pairs(cb_context *c, int32_t *i, int32_t *j, int32_t capacity, int32_
 }
 
 int cb_set_pairs(cb_context *c, const int32_t *i, const int32_t *j, int32_t count) {
+    {
+        if (!c) return fail(CB_ERR_INVALID_ARGUMENT, "null context");
+        CB_CUDA(cudaSetDevice(c->dev));
+        const int rc0 = invalidate_prediction(c);
+        if (rc0) return rc0;
+    }
     CB_ENTER(c);
     if (count < 0 || (count && (!i || !j))) return fail(CB_ERR_INVALID_ARGUMENT, "bad pairs");
     if (count > c->hk.pcap) return fail(CB_ERR_CAPACITY, "pair capacity exceeded");

@@ -13,7 +13,7 @@ const char *status_text(int s);
 // Kernels per phase (for the launch counter of graph executions).
 constexpr int kKernelsPerAttempt = 3;
 constexpr int kKernelsPerRemove = 9;
-constexpr int kKernelsPerSearch = 15;
+constexpr int kKernelsPerSearch = 16;
 }  // namespace cbg
 
 #define CB_CUDA(x)                                                                          \
@@ -89,6 +89,7 @@ struct cb_context {
 
 namespace cbg {
 int sync_status(cb_context *c);
+int invalidate_prediction(cb_context *c);
 void launch_attempt_kernels(const cb_context *c, const Launch &l, const Bufs &b, int which = 7);
 int capture_conditional(cudaStream_t stream, cudaGraphConditionalNodeType type,
                         cudaGraphConditionalHandle *handle, unsigned int dflt,

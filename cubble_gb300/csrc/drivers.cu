@@ -112,6 +112,8 @@ extern "C" {
 int cb_transform_positions(cb_context *c, int32_t normalize) {
     CB_ENTER(c);
     if (!c->loaded) return fail(CB_ERR_STATE, "state not loaded");
+    int rc0 = invalidate_prediction(c);
+    if (rc0) return rc0;
     k_transform<<<c->launch.grid, kBlock, 0, c->stream>>>(c->bufs, normalize ? 1 : 0);
     c->launches += 1;
     CB_CUDA(cudaGetLastError());

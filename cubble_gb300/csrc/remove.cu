@@ -100,6 +100,8 @@ __device__ __forceinline__ void k_remove_c_body(const Bufs &b, const int vb, con
         c->delete_events += 1;
         c->ndel = 0;
         c->need_delete = 0;
+        c->pred_ready = 0;  // bubbles moved and radii rescaled
+        c->pred_slot = 0;
         c->done[DC_REMOVE] = 0;
     }
 }

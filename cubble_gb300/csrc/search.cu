@@ -10,12 +10,15 @@
 //                 saved := positions (reorganizeByIndex, src/kernels.cu:721-770);
 //                 the pointer rotation of src/simulator.cu:99-146 becomes a
 //                 role swap in the control block
-//   k_pair_rows   per bubble, the pairs (i, j > i) within r_i + r_j + skin
+//   k_pair_cells  per bubble, the pairs (i, j > i) within r_i + r_j + skin
 //                 (neighborSearch / comparePair, src/kernels.cu:617-701):
-//                 a count pass, a scan, a fill pass, so the list is ordered
-//                 by (i, j) without atomics; candidates are screened in FP32
-//                 with a conservative margin and accepted by the exact FP64
-//                 test of the reference, so the pair set is bit-exact
+//                 one enumeration that counts each row and keeps its
+//                 partners, a scan, k_pair_compact writing the rows, so the
+//                 list is ordered by (i, j) without atomics (a second
+//                 enumeration only when a row outgrew its stash); candidates
+//                 are screened in FP32 with a conservative margin and
+//                 accepted by the exact FP64 test of the reference, so the
+//                 pair set is bit-exact
 //   k_degree      neighbour counts (countNumNeighbors, src/kernels.cu:713-719)
 #include "common.cuh"
 
@@ -92,6 +95,9 @@ __device__ __forceinline__ void k_wrap_body(const Bufs &b, const int vb, const i
             c->cell_dims[2] = cd[2];
             c->ncell = cd[0] * cd[1] * cd[2];
             c->searches += 1;
+            c->stash_over = 0;
+            c->pred_ready = 0;  // the bubbles move to new slots
+            c->pred_slot = 0;
             c->done[DC_WRAP] = 0;
         }
     }
@@ -308,11 +314,17 @@ constexpr int kWarpsPerBlock = kBlock / 32;
 // unless its distance lies within the guard band `pre_margin` of the cutoff;
 // only there the exact FP64 test of comparePair (src/kernels.cu:619-623)
 // runs, so the pair set equals the FP64 one bit for bit.
-// WRITE = false counts rows, WRITE = true writes them at rowStart.
+// WRITE = false counts rows and keeps the first kStash partners of each row
+// in `stash` (k_pair_compact then writes the list without a second
+// enumeration); WRITE = true, needed only when some row had more partners,
+// enumerates again and writes the rows at rowStart.
 template <int DIM, bool WRITE>
 __device__ __forceinline__ void k_pair_cells_body(const Bufs &b, const int vb, const int vg) {
     __shared__ float4 stage[kWarpsPerBlock][32];
     Ctrl *c = b.ctrl;
+    if (WRITE && !c->stash_over) return;  // k_pair_compact wrote the list
+    constexpr int M = kStash(DIM);
+    bool over = false;
     const DevConst &k = *b.k;
     const int ncell = c->ncell;
     const int cd[3] = {c->cell_dims[0], c->cell_dims[1], c->cell_dims[2]};
@@ -381,20 +393,26 @@ __device__ __forceinline__ void k_pair_cells_body(const Bufs &b, const int vb, c
                                 PI[base + cnt] = i;
                                 PJ[base + cnt] = j;
                             }
+                            if (!WRITE && cnt < M) b.stash[(size_t)i * M + cnt] = j;
                             cnt++;
                         }
                     }
                 }
             }
             if (active) {
-                if (WRITE)
-                    NN[i] = cnt;
-                else
+                NN[i] = cnt;
+                if (!WRITE) {
                     b.rowCount[i] = cnt;
+                    over |= cnt > M;
+                }
             }
         }
     }
-    if (WRITE && last_block(&c->done[DC_MISC], vg) && threadIdx.x == 0) {
+    if (!WRITE) {
+        if (__syncthreads_or(over) && threadIdx.x == 0) atomicOr(&c->stash_over, 1);
+        return;
+    }
+    if (last_block(&c->done[DC_MISC], vg) && threadIdx.x == 0) {
         const int found = c->np_found;
         if (found > pcap) {
             c->status = CB_ERR_CAPACITY;
@@ -407,6 +425,41 @@ __device__ __forceinline__ void k_pair_cells_body(const Bufs &b, const int vb, c
     }
 }
 CB_KERNEL_PAIR((template <int DIM, bool WRITE>), k_pair_cells, (<DIM, WRITE>), __launch_bounds__(kBlock))
+
+// The pair list from the counting pass's stash: row i's partners go to
+// rowStart[i] .. rowStart[i] + rowCount[i] (pairs grouped by i, j ascending
+// inside a row as the enumeration found them). Skipped when a row
+// overflowed its stash (the WRITE pass then writes the list).
+template <int DIM>
+__device__ __forceinline__ void k_pair_compact_body(const Bufs &b, const int vb, const int vg) {
+    Ctrl *c = b.ctrl;
+    if (c->stash_over) return;
+    constexpr int M = kStash(DIM);
+    const int n = c->n;
+    const int pcap = b.k->pcap;
+    int *PI = b.ps[c->prole[PI0]];
+    int *PJ = b.ps[c->prole[PJ0]];
+    for (int i = vb * blockDim.x + threadIdx.x; i < n; i += vg * blockDim.x) {
+        const int base = b.rowStart[i], cnt = b.rowCount[i];
+        const int *src = b.stash + (size_t)i * M;
+        for (int t = 0; t < cnt && base + t < pcap; t++) {
+            PI[base + t] = i;
+            PJ[base + t] = src[t];
+        }
+    }
+    if (last_block(&c->done[DC_MISC], vg) && threadIdx.x == 0) {
+        const int found = c->np_found;
+        if (found > pcap) {
+            c->status = CB_ERR_CAPACITY;
+            c->np = 0;
+        } else {
+            c->np = found;
+        }
+        c->need_search = 0;
+        c->done[DC_MISC] = 0;
+    }
+}
+CB_KERNEL_PAIR((template <int DIM>), k_pair_compact, (<DIM>), __launch_bounds__(kBlock))
 
 
 __device__ __forceinline__ void k_degree_body(const Bufs &b, const int vb, const int vg) {
@@ -444,10 +497,13 @@ void launch_search(const Launch &l, const Bufs &b, int dim) {
         CB_LAUNCH(l, k_pair_cells, (<2, false>), G, b);
     }
     launch_scan(l, b, SCAN_ROWS);
-    if (dim == 3)
+    if (dim == 3) {
+        CB_LAUNCH(l, k_pair_compact, (<3>), G, b);
         CB_LAUNCH(l, k_pair_cells, (<3, true>), G, b);
-    else
+    } else {
+        CB_LAUNCH(l, k_pair_compact, (<2>), G, b);
         CB_LAUNCH(l, k_pair_cells, (<2, true>), G, b);
+    }
     CB_LAUNCH(l, k_degree, (), G, b);
 }
 

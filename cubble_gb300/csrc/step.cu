@@ -127,45 +127,46 @@ __device__ __forceinline__ void k_pairs_body(const Bufs &b, const int vb, const 
         m = fma(dy, dy, m);
         if (DIM == 3) m = fma(dz, dz, m);
         const double radii = r1 + r2;
-        if (fma(radii, radii, -m) >= 0.0) {
+        // overlap test radii^2 >= m on the sign of the exact difference
+        if (nonneg_bits(fma(radii, radii, -m))) {
             // velocity f0 d (1/|d| - 1/(r1 + r2)), src/kernels.cu:218-233
             const double rs = rsqrt_hn(m);
             const double s = f0 * (rs - rcp_hn(radii));
             const double fx = dx * s, fy = dy * s;
             atomicAdd(ai + 0, fx);
-            atomicAdd(aj + 0, -fx);
+            atomicAdd(aj + 0, neg_bits(fx));
             atomicAdd(ai + 1, fy);
-            atomicAdd(aj + 1, -fy);
+            atomicAdd(aj + 1, neg_bits(fy));
             if (DIM == 3) {
                 const double fz = dz * s;
                 atomicAdd(ai + 2, fz);
-                atomicAdd(aj + 2, -fz);
+                atomicAdd(aj + 2, neg_bits(fz));
             }
             if (GAS) {  // pairwise gas exchange, src/kernels.cu:236-280
                 const double r1sq = r1 * r1, r2sq = r2 * r2;
-                const bool inside = m < r1sq || m < r2sq;
+                const bool inside = less_nonneg(m, r1sq) || less_nonneg(m, r2sq);
                 double oa;
                 if (DIM == 3) {
                     if (inside) {
-                        oa = fmin(r1sq, r2sq);
+                        oa = min_nonneg(r1sq, r2sq);
                     } else {
                         const double t = 0.5 * (r2sq - r1sq + m);
-                        oa = fabs(r2sq - (t * t) * (rs * rs));
+                        oa = abs_bits(r2sq - (t * t) * (rs * rs));
                     }
                     oa *= kPi;
                 } else {
                     if (inside) {
-                        oa = 2.0 * fmin(r1, r2);
+                        oa = 2.0 * min_nonneg(r1, r2);
                     } else {
                         const double t = 0.5 * (r2sq - r1sq + m);
-                        oa = 2.0 * sqrt_hn(fabs(r2sq - (t * t) * (rs * rs)));
+                        oa = 2.0 * sqrt_hn(abs_bits(r2sq - (t * t) * (rs * rs)));
                     }
                 }
                 const double inv1 = DIM == 3 ? b.invr[i] : a.w;
                 const double inv2 = DIM == 3 ? b.invr[j] : q.w;
                 const double g = oa * (inv2 - inv1);
                 atomicAdd(ai + 3, g);
-                atomicAdd(aj + 3, -g);
+                atomicAdd(aj + 3, neg_bits(g));
                 atomicAdd(ai + 4, oa);
                 atomicAdd(aj + 4, oa);
                 sAo += oa;

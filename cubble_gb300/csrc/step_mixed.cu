@@ -131,8 +131,8 @@ struct __align__(16) PredMx {
     float r, inv;
 };
 
-__device__ __forceinline__ PredMx ld_pred(const Bufs &b, int i) {
-    const longlong2 *p = reinterpret_cast<const longlong2 *>(b.pred) + 2 * (size_t)i;
+__device__ __forceinline__ PredMx ld_pred(const double *base, int i) {
+    const longlong2 *p = reinterpret_cast<const longlong2 *>(base) + 2 * (size_t)i;
     const longlong2 u = p[0], v = p[1];
     PredMx r;
     r.q[0] = u.x;
@@ -143,18 +143,28 @@ __device__ __forceinline__ PredMx ld_pred(const Bufs &b, int i) {
     return r;
 }
 
-__device__ __forceinline__ void st_pred(const Bufs &b, int i, const PredMx &r) {
-    longlong2 *p = reinterpret_cast<longlong2 *>(b.pred) + 2 * (size_t)i;
+__device__ __forceinline__ void st_pred(double *base, int i, const PredMx &r) {
+    longlong2 *p = reinterpret_cast<longlong2 *>(base) + 2 * (size_t)i;
     p[0] = make_longlong2(r.q[0], r.q[1]);
     p[1] = make_longlong2(r.q[2], (long long)(unsigned int)__float_as_int(r.r) |
                                       ((long long)__float_as_int(r.inv) << 32));
 }
 
+// The prediction the coming attempt uses: slot 0 (k_predict_mx) or one of
+// the two candidates the last correct wrote.
+__device__ __forceinline__ const double *pred_base(const Bufs &b, const Ctrl *c, int cap) {
+    const int s = c->pred_slot;
+    return s == 0 ? b.pred : b.predc + (size_t)(s - 1) * 4 * cap;
+}
+
 // ---------------------------------------------------------------- predict
+// Skipped (every block returns at once) when the last correct already
+// wrote this attempt's prediction and its area sums.
 template <int DIM>
 __device__ __forceinline__ void k_predict_mx_body(const Bufs &b, const int vb, const int vg) {
     __shared__ double smem[32];
     const Ctrl *c = b.ctrl;
+    if (c->pred_ready) return;
     const int n = c->n;
     const float h = float_from_double(0.5 * c->dt);
     const int gas = c->use_gas;
@@ -165,22 +175,45 @@ __device__ __forceinline__ void k_predict_mx_body(const Bufs &b, const int vb, c
     const float *O0 = frow(b, c, RVO0), *O1 = frow(b, c, RVO1), *O2 = frow(b, c, RVO2),
                 *O3 = frow(b, c, RVO3);
     float sA = 0.f, sAr = 0.f;
-    for (int i = vb * blockDim.x + threadIdx.x; i < n; i += vg * blockDim.x) {
-        // AB2 increment h (3 v - vo) in FP32 on the fixed point of x
-        PredMx p;
-        p.q[0] = fix_from_double(X[i]) + fix_from_float(h * fmaf(3.f, V0[i], -O0[i]));
-        p.q[1] = fix_from_double(Y[i]) + fix_from_float(h * fmaf(3.f, V1[i], -O1[i]));
-        p.q[2] = DIM == 3 ? fix_from_double(Z[i]) + fix_from_float(h * fmaf(3.f, V2[i], -O2[i]))
-                          : 0LL;
-        float rp = float_from_double(R[i]);
-        if (gas) rp = fmaf(h, fmaf(3.f, V3[i], -O3[i]), rp);
-        p.r = rp;
-        p.inv = 1.f / rp;
-        st_pred(b, i, p);
-        if (gas) {
-            const float apr = DIM == 3 ? (4.f * (float)kPi) * rp : 2.f * (float)kPi;
-            sA = fmaf(apr, rp, sA);
-            sAr += apr;
+    // two bubbles per iteration, all loads of both issued before any store
+    // (twice the loads in flight of a one-bubble loop)
+    const int stride = vg * blockDim.x;
+    for (int i0 = vb * blockDim.x + threadIdx.x; i0 < n; i0 += 2 * stride) {
+        const int i1 = i0 + stride < n ? i0 + stride : i0;
+        const int ii[2] = {i0, i1};
+        double x[2], y[2], z[2], r[2];
+        float d[4][2];
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int i = ii[u];
+            x[u] = __ldg(X + i);
+            y[u] = __ldg(Y + i);
+            z[u] = DIM == 3 ? __ldg(Z + i) : 0.0;
+            r[u] = __ldg(R + i);
+            // AB2 direction 3 v - vo
+            d[0][u] = fmaf(3.f, __ldg(V0 + i), -__ldg(O0 + i));
+            d[1][u] = fmaf(3.f, __ldg(V1 + i), -__ldg(O1 + i));
+            d[2][u] = DIM == 3 ? fmaf(3.f, __ldg(V2 + i), -__ldg(O2 + i)) : 0.f;
+            d[3][u] = gas ? fmaf(3.f, __ldg(V3 + i), -__ldg(O3 + i)) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            if (u == 1 && ii[1] == ii[0]) break;
+            // AB2 increment h (3 v - vo) in FP32 on the fixed point of x
+            PredMx p;
+            p.q[0] = fix_from_double(x[u]) + fix_from_float(h * d[0][u]);
+            p.q[1] = fix_from_double(y[u]) + fix_from_float(h * d[1][u]);
+            p.q[2] = DIM == 3 ? fix_from_double(z[u]) + fix_from_float(h * d[2][u]) : 0LL;
+            float rp = float_from_double(r[u]);
+            if (gas) rp = fmaf(h, d[3][u], rp);
+            p.r = rp;
+            p.inv = 1.f / rp;
+            st_pred(b.pred, ii[u], p);
+            if (gas) {
+                const float apr = DIM == 3 ? (4.f * (float)kPi) * rp : 2.f * (float)kPi;
+                sA = fmaf(apr, rp, sA);
+                sAr += apr;
+            }
         }
     }
     const double tA = block_sum_f(sA, smem);
@@ -228,6 +261,7 @@ __device__ __forceinline__ void k_pairs_mx_body(const Bufs &b, const int vb, con
     const bool px = !k.wall[0], py = !k.wall[1], pz = DIM == 3 && !k.wall[2];
     const long long hx = k.hq[0], hy = k.hq[1], hz = k.hq[2];
     const long long lx = k.lq[0], ly = k.lq[1], lz = k.lq[2];
+    const double *PB = pred_base(b, c, cap);
     float sAo = 0.f, sAor = 0.f;
     const int nrun = (np + kRun - 1) / kRun;
     for (int g = vb * blockDim.x + threadIdx.x; g < nrun; g += vg * blockDim.x) {
@@ -266,7 +300,7 @@ __device__ __forceinline__ void k_pairs_mx_body(const Bufs &b, const int vb, con
             if (i != cur) {
                 if (hit) flush();
                 cur = i;
-                a = ld_pred(b, i);
+                a = ld_pred(PB, i);
                 ax = ay = az = ag = ao = 0.f;
                 fx_i = fy_i = fz_i = 0.f;
                 hit = false;
@@ -278,7 +312,7 @@ __device__ __forceinline__ void k_pairs_mx_body(const Bufs &b, const int vb, con
             }
             if (FLOW)  // src/kernels.cu:191-207 (added for every pair)
                 red_add4(AF + j, vxi, vyi, vzi, 0.f);
-            const PredMx q = ld_pred(b, j);
+            const PredMx q = ld_pred(PB, j);
             long long ex = a.q[0] - q.q[0], ey = a.q[1] - q.q[1], ez = 0;
             if (px) ex = wrap_fix(ex, hx, lx);
             if (py) ey = wrap_fix(ey, hy, ly);
@@ -391,6 +425,7 @@ struct CorrRed {
     long long err, rad, exp;
     double vol;
     int del, bad;
+    float cA[2], cAr[2];  // area sums of the two candidate predictions
 };
 
 __device__ __forceinline__ CorrRed block_reduce_corr(CorrRed v, CorrRed *smem) {
@@ -403,6 +438,11 @@ __device__ __forceinline__ CorrRed block_reduce_corr(CorrRed v, CorrRed *smem) {
         v.vol += __shfl_down_sync(0xffffffffu, v.vol, o);
         v.del += __shfl_down_sync(0xffffffffu, v.del, o);
         v.bad += __shfl_down_sync(0xffffffffu, v.bad, o);
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            v.cA[u] += __shfl_down_sync(0xffffffffu, v.cA[u], o);
+            v.cAr[u] += __shfl_down_sync(0xffffffffu, v.cAr[u], o);
+        }
     }
     if (lane == 0) smem[warp] = v;
     __syncthreads();
@@ -415,6 +455,11 @@ __device__ __forceinline__ CorrRed block_reduce_corr(CorrRed v, CorrRed *smem) {
             v.vol += u.vol;
             v.del += u.del;
             v.bad += u.bad;
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                v.cA[q] += u.cA[q];
+                v.cAr[q] += u.cAr[q];
+            }
         }
     return v;
 }
@@ -446,6 +491,9 @@ __device__ __forceinline__ void k_correct_mx_body(const Bufs &b, const int vb, c
     const float kq = k.kq_f;
     const long long minr = __double_as_longlong(k.min_rad);
     const bool shear = c->use_flow && k.shear_on;
+    // the two dt the next attempt can have after an accept (finish_attempt)
+    const float hI = float_from_double(0.5 * (c->dt * 1.269));
+    float cA0 = 0.f, cA1 = 0.f, cAr0 = 0.f, cAr1 = 0.f;
     long long merr = 0, mrad = 0;
     float mexp = 0.f;
     double vol = 0.0;
@@ -536,6 +584,7 @@ __device__ __forceinline__ void k_correct_mx_body(const Bufs &b, const int vb, c
         const float dz = DIM == 3 ? float_from_double(cz - CB_D(RS2)[i]) : 0.f;
         float dist = sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
         int del = 0;
+        double cr_keep = r0;
         if (GAS) {  // mean-field gas exchange, src/kernels.cu:390-431
             const float inv = 1.f / rp;
             const float area = DIM == 3 ? (4.f * (float)kPi) * (rp * rp) : (2.f * (float)kPi) * rp;
@@ -544,6 +593,7 @@ __device__ __forceinline__ void k_correct_mx_body(const Bufs &b, const int vb, c
             vpr = w;
             const float ir = h * (vr + w);
             const double cr = r0 + double_from_float(ir);
+            cr_keep = cr;
             e = fmaxf(e, fabsf(fmaf(2.f, vr, -or_) - w));
             dist += float_from_double(cr - CB_D(RS3)[i]);
             if (__double_as_longlong(cr) > minr) {
@@ -576,6 +626,37 @@ __device__ __forceinline__ void k_correct_mx_body(const Bufs &b, const int vb, c
             CB_F(RVP2)[i] = vpz;
         }
         bad |= !(finite_bits(cx) && finite_bits(cy) && finite_bits(cz));
+        {  // the next attempt's prediction, as k_predict_mx would compute it
+           // from the rotated state, for both dt: x' = cx, v' = vp, vo' = v
+            const long long q0 = fix_from_double(cx), q1 = fix_from_double(cy);
+            const long long q2 = DIM == 3 ? fix_from_double(cz) : 0LL;
+            const float d0 = fmaf(3.f, vpx, -vx), d1 = fmaf(3.f, vpy, -vy);
+            const float d2 = DIM == 3 ? fmaf(3.f, vpz, -vz) : 0.f;
+            const float rb = float_from_double(GAS ? cr_keep : r0);
+            const float d3 = GAS ? fmaf(3.f, vpr, -vr) : 0.f;
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const float hh = u ? hI : h;
+                PredMx p;
+                p.q[0] = q0 + fix_from_float(hh * d0);
+                p.q[1] = q1 + fix_from_float(hh * d1);
+                p.q[2] = DIM == 3 ? q2 + fix_from_float(hh * d2) : 0LL;
+                const float rp1 = GAS ? fmaf(hh, d3, rb) : rb;
+                p.r = rp1;
+                p.inv = 1.f / rp1;
+                st_pred(b.predc + (size_t)u * 4 * cap, i, p);
+                if (GAS) {
+                    const float apr = DIM == 3 ? (4.f * (float)kPi) * rp1 : 2.f * (float)kPi;
+                    if (u) {
+                        cA1 = fmaf(apr, rp1, cA1);
+                        cAr1 += apr;
+                    } else {
+                        cA0 = fmaf(apr, rp1, cA0);
+                        cAr0 += apr;
+                    }
+                }
+            }
+        }
         if (b.dbg_ov) b.dbg_ov[i] = double_from_float(ovl);
         AV[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         if (GAS && DIM == 3) AO[i] = 0.f;
@@ -583,9 +664,16 @@ __device__ __forceinline__ void k_correct_mx_body(const Bufs &b, const int vb, c
     }
 #undef CB_D
 #undef CB_F
-    CorrRed v{merr, mrad, __double_as_longlong(double_from_float(mexp)), vol, ndel, bad};
+    CorrRed v{merr, mrad, __double_as_longlong(double_from_float(mexp)), vol, ndel, bad,
+              {cA0, cA1}, {cAr0, cAr1}};
     v = block_reduce_corr(v, rsm);
     if (threadIdx.x == 0) {
+        if (GAS) {
+            atomicAdd(&c->cand_sumA[0], (double)v.cA[0]);
+            atomicAdd(&c->cand_sumA[1], (double)v.cA[1]);
+            atomicAdd(&c->cand_sumAr[0], (double)v.cAr[0]);
+            atomicAdd(&c->cand_sumAr[1], (double)v.cAr[1]);
+        }
         atomicMax(&c->amax_err, v.err);
         atomicMax(&c->amax_rad, v.rad);
         atomicMax(&c->amax_exp, v.exp);
@@ -631,17 +719,17 @@ __global__ void __launch_bounds__(kBlock) k_boot_mx(Bufs b, int phase) {
             p.q[2] = DIM == 3 ? fix_from_double(Z[i]) : 0LL;
             p.r = float_from_double(R[i]);
             p.inv = 1.f / p.r;
-            st_pred(b, i, p);
+            st_pred(b.pred, i, p);
             O0[i] = O1[i] = O2[i] = O3[i] = 0.f;
             PATH[i] = 0.0;
         } else {
             const float4 a = AV[i];
             if (phase == 1) {
-                PredMx p = ld_pred(b, i);
+                PredMx p = ld_pred(b.pred, i);
                 p.q[0] += fix_from_float(a.x * ts);
                 p.q[1] += fix_from_float(a.y * ts);
                 if (DIM == 3) p.q[2] += fix_from_float(a.z * ts);
-                st_pred(b, i, p);
+                st_pred(b.pred, i, p);
             } else {
                 O0[i] = a.x;
                 O1[i] = a.y;

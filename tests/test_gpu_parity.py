@@ -68,6 +68,27 @@ def test_search_bit_exact(oracle_mod, case):
     assert set(zip(gi.tolist(), gj.tolist())) == brute_pairs(cfg, sg)
 
 
+@pytest.mark.parametrize("dim", [2, 3])
+def test_search_rows_beyond_stash(oracle_mod, dim):
+    """Rows with more partners than the counting pass keeps (a few large
+    bubbles among small ones) take the second enumeration; the pair list is
+    still the oracle's, bit for bit."""
+    n = 3000 if dim == 2 else 4000
+    cfg, st = workloads.foam(n, dim, 0.85, rmean=0.4, rstd=0.05, rclip=(0.3, 0.5), seed=107)
+    r = st["r"].copy()
+    r[:: n // 5] = 4.0  # five large bubbles
+    st["r"] = r
+    g, o = pair_both(oracle_mod, cfg, st)
+    g.search_neighbors()
+    o.search_neighbors()
+    gi, gj = g.pairs()
+    oi, oj = o.pairs()
+    counts = np.bincount(oi, minlength=n)
+    assert counts.max() > (16 if dim == 2 else 32)
+    assert np.array_equal(gi, oi) and np.array_equal(gj, oj)
+    int_rows_equal(g.get_state(), o.get_state())
+
+
 @pytest.mark.parametrize("case", ["2d", "3d", "2d-wallx", "3d-wallz"])
 def test_bootstrap_and_attempt(oracle_mod, case):
     cfg, st = make(case)
