@@ -13,7 +13,7 @@ const char *status_text(int s);
 // Kernels per phase (for the launch counter of graph executions).
 constexpr int kKernelsPerAttempt = 3;
 constexpr int kKernelsPerRemove = 9;
-constexpr int kKernelsPerSearch = 16;
+constexpr int kKernelsPerSearch = 17;
 }  // namespace cbg
 
 #define CB_CUDA(x)                                                                          \

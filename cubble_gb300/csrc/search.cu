@@ -96,6 +96,7 @@ __device__ __forceinline__ void k_wrap_body(const Bufs &b, const int vb, const i
             c->ncell = cd[0] * cd[1] * cd[2];
             c->searches += 1;
             c->stash_over = 0;
+            c->sparse_cells = (long long)c->n < 8LL * c->ncell;
             c->pred_ready = 0;  // the bubbles move to new slots
             c->pred_slot = 0;
             c->done[DC_WRAP] = 0;
@@ -307,6 +308,39 @@ __device__ __forceinline__ int warp_sort(int v) {
 
 constexpr int kWarpsPerBlock = kBlock / 32;
 
+// Is j a pair partner of i (comparePair, src/kernels.cu:619-623)? Decided in
+// FP32 unless the distance lies within the guard band `pre_margin` of the
+// cutoff; there the reference's exact FP64 test decides (i's FP64 position
+// is loaded once, on first need, into xi..ri).
+template <int DIM>
+__device__ __forceinline__ bool pair_take(const DevConst &k, const float4 &pi, const float4 &pj,
+                                          int i, int j, const double *X, const double *Y,
+                                          const double *Z, const double *R, double &xi,
+                                          double &yi, double &zi, double &ri) {
+    const bool per[3] = {!k.wall[0], !k.wall[1], !k.wall[2]};
+    float dx = fabsf(pi.x - pj.x), dy = fabsf(pi.y - pj.y);
+    float dz = DIM == 3 ? fabsf(pi.z - pj.z) : 0.f;
+    if (per[0] && dx > k.half_iv32[0]) dx = k.iv32[0] - dx;
+    if (per[1] && dy > k.half_iv32[1]) dy = k.iv32[1] - dy;
+    if (DIM == 3 && per[2] && dz > k.half_iv32[2]) dz = k.iv32[2] - dz;
+    float d2 = fmaf(dx, dx, dy * dy);
+    if (DIM == 3) d2 = fmaf(dz, dz, d2);
+    const float cut = pi.w + pj.w + (float)k.skin;
+    const float band = k.pre_margin;
+    const float hi = cut + band, lo = fmaxf(cut - band, 0.f);
+    if (d2 >= hi * hi) return false;
+    if (d2 < lo * lo) return true;
+    if (ri == 0.0) {
+        xi = X[i];
+        yi = Y[i];
+        zi = DIM == 3 ? Z[i] : 0.0;
+        ri = R[i];
+    }
+    const double maxd = __dadd_rn(__dadd_rn(ri, R[j]), k.skin);
+    const double sq = exact_sqdist<DIM>(k, xi, yi, zi, X[j], Y[j], DIM == 3 ? Z[j] : 0.0);
+    return sq < __dmul_rn(maxd, maxd);
+}
+
 // Pair rows of one cell per warp: lanes are the cell's bubbles (32 at a
 // time); each neighbour cell with a linear index >= the home cell is staged
 // 32 bubbles at a time in shared memory (FP32 x, y, z, r) and every lane
@@ -323,6 +357,7 @@ __device__ __forceinline__ void k_pair_cells_body(const Bufs &b, const int vb, c
     __shared__ float4 stage[kWarpsPerBlock][32];
     Ctrl *c = b.ctrl;
     if (WRITE && !c->stash_over) return;  // k_pair_compact wrote the list
+    if (!WRITE && c->sparse_cells) return;  // k_pair_rows counts sparse grids
     constexpr int M = kStash(DIM);
     bool over = false;
     const DevConst &k = *b.k;
@@ -335,8 +370,6 @@ __device__ __forceinline__ void k_pair_cells_body(const Bufs &b, const int vb, c
     int *NN = irow(b, c, INN);
     const int pcap = k.pcap;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const float skin32 = (float)k.skin, band = k.pre_margin;
-    const bool per[3] = {!k.wall[0], !k.wall[1], !k.wall[2]};
     const int warps = vg * kWarpsPerBlock;
     for (int cell = vb * kWarpsPerBlock + w; cell < ncell; cell += warps) {
         const int s0 = b.cellStart[cell], e0 = b.cellStart[cell + 1];
@@ -365,29 +398,7 @@ __device__ __forceinline__ void k_pair_cells_body(const Bufs &b, const int vb, c
                         const int j = c0 + t;
                         const float4 pj = stage[w][t];
                         if (!active || j <= i) continue;
-                        float dx = fabsf(pi.x - pj.x), dy = fabsf(pi.y - pj.y);
-                        float dz = DIM == 3 ? fabsf(pi.z - pj.z) : 0.f;
-                        if (per[0] && dx > k.half_iv32[0]) dx = k.iv32[0] - dx;
-                        if (per[1] && dy > k.half_iv32[1]) dy = k.iv32[1] - dy;
-                        if (DIM == 3 && per[2] && dz > k.half_iv32[2]) dz = k.iv32[2] - dz;
-                        float d2 = fmaf(dx, dx, dy * dy);
-                        if (DIM == 3) d2 = fmaf(dz, dz, d2);
-                        const float cut = pi.w + pj.w + skin32;
-                        const float hi = cut + band, lo = fmaxf(cut - band, 0.f);
-                        if (d2 >= hi * hi) continue;
-                        bool take = d2 < lo * lo;
-                        if (!take) {
-                            if (ri == 0.0) {
-                                xi = X[i];
-                                yi = Y[i];
-                                zi = DIM == 3 ? Z[i] : 0.0;
-                                ri = R[i];
-                            }
-                            const double maxd = __dadd_rn(__dadd_rn(ri, R[j]), k.skin);
-                            const double sq = exact_sqdist<DIM>(k, xi, yi, zi, X[j], Y[j],
-                                                                DIM == 3 ? Z[j] : 0.0);
-                            take = sq < __dmul_rn(maxd, maxd);
-                        }
+                        const bool take = pair_take<DIM>(k, pi, pj, i, j, X, Y, Z, R, xi, yi, zi, ri);
                         if (take) {
                             if (WRITE && base + cnt < pcap) {
                                 PI[base + cnt] = i;
@@ -425,6 +436,62 @@ __device__ __forceinline__ void k_pair_cells_body(const Bufs &b, const int vb, c
     }
 }
 CB_KERNEL_PAIR((template <int DIM, bool WRITE>), k_pair_cells, (<DIM, WRITE>), __launch_bounds__(kBlock))
+
+// Counting pass for sparse cell grids (fewer than 8 bubbles per cell on
+// average, e.g. 2D foams): one thread per bubble walks its neighbour cells
+// >= its own cell in ascending order and the bubbles j > i in them, so the
+// rows and their order are those of the warp-per-cell pass, with all lanes
+// busy (a warp per cell of ~3 bubbles would leave 90 % of its lanes idle).
+template <int DIM>
+__device__ __forceinline__ void k_pair_rows_body(const Bufs &b, const int vb, const int vg) {
+    Ctrl *c = b.ctrl;
+    if (!c->sparse_cells) return;
+    const DevConst &k = *b.k;
+    constexpr int M = kStash(DIM);
+    constexpr int NO = DIM == 3 ? 27 : 9;  // stencil offsets
+    const int n = c->n;
+    const int cd[3] = {c->cell_dims[0], c->cell_dims[1], c->cell_dims[2]};
+    const double *X = drow(b, c, RX), *Y = drow(b, c, RY), *Z = drow(b, c, RZ),
+                 *R = drow(b, c, RR);
+    int *NN = irow(b, c, INN);
+    bool over = false;
+    for (int i = vb * blockDim.x + threadIdx.x; i < n; i += vg * blockDim.x) {
+        const int cell = b.cellSorted[i];
+        int nb[NO];
+        int nq = 0;
+#pragma unroll
+        for (int t = 0; t < NO; t++) {
+            const int o = DIM == 3 ? t : 9 + t;  // 2D: the z-offset-0 plane
+            const int v = neighbor_cell<DIM>(k, cd, cell, o);
+            if (v != 0x7fffffff) {
+                int p = nq++;  // insertion into the ascending list
+                while (p > 0 && nb[p - 1] > v) {
+                    nb[p] = nb[p - 1];
+                    p--;
+                }
+                nb[p] = v;
+            }
+        }
+        const float4 pi = b.pos32[i];
+        double xi = 0.0, yi = 0.0, zi = 0.0, ri = 0.0;
+        int cnt = 0;
+        for (int t = 0; t < nq; t++) {
+            const int q = nb[t];
+            const int ce = b.cellStart[q + 1];
+            for (int j = max(b.cellStart[q], i + 1); j < ce; j++) {
+                if (pair_take<DIM>(k, pi, b.pos32[j], i, j, X, Y, Z, R, xi, yi, zi, ri)) {
+                    if (cnt < M) b.stash[(size_t)i * M + cnt] = j;
+                    cnt++;
+                }
+            }
+        }
+        NN[i] = cnt;
+        b.rowCount[i] = cnt;
+        over |= cnt > M;
+    }
+    if (__syncthreads_or(over) && threadIdx.x == 0) atomicOr(&c->stash_over, 1);
+}
+CB_KERNEL_PAIR((template <int DIM>), k_pair_rows, (<DIM>), __launch_bounds__(kBlock))
 
 // The pair list from the counting pass's stash: row i's partners go to
 // rowStart[i] .. rowStart[i] + rowCount[i] (pairs grouped by i, j ascending
@@ -491,10 +558,12 @@ void launch_search(const Launch &l, const Bufs &b, int dim) {
         CB_LAUNCH(l, k_permute_a, (<3>), G, b);
         CB_LAUNCH(l, k_permute_b, (<3>), G, b);
         CB_LAUNCH(l, k_pair_cells, (<3, false>), G, b);
+        CB_LAUNCH(l, k_pair_rows, (<3>), G, b);
     } else {
         CB_LAUNCH(l, k_permute_a, (<2>), G, b);
         CB_LAUNCH(l, k_permute_b, (<2>), G, b);
         CB_LAUNCH(l, k_pair_cells, (<2, false>), G, b);
+        CB_LAUNCH(l, k_pair_rows, (<2>), G, b);
     }
     launch_scan(l, b, SCAN_ROWS);
     if (dim == 3) {
