@@ -24,6 +24,7 @@
 //                            run per parameter set, each in run_<k>/.
 #include <cuda_runtime.h>
 #include <curand.h>
+#include <nvtx3/nvToolsExt.h>
 #include <sys/stat.h>
 #include <unistd.h>
 
@@ -117,11 +118,28 @@ cb_report report(Run &r) {
 // stabilize(), src/simulator.cu:338-360: n steps without gas exchange, flow
 // or path, energies before and after.
 void stabilize(Run &r, int32_t n) {
+    nvtxRangePushA("Stabilization");
     r.energy1 = energy(r);
     check(cb_set_options(r.ctx, 0, 0, 0), "cb_set_options");
     cb_report rep{};
     check(cb_integrate(r.ctx, n, &rep), "cb_integrate");
     r.energy2 = energy(r);
+    nvtxRangePop();
+}
+
+// printRelevantInfoOfCurrentDevice, src/util.cuh:222-251
+void print_device() {
+    int dev = 0;
+    cudaDeviceProp p{};
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&p, dev) != cudaSuccess)
+        return;
+    std::printf("\n---------------Properties of current device----------------");
+    std::printf("\n\tName: %s\n\tCompute capability: %d.%d", p.name, p.major, p.minor);
+    std::printf("\n\tMultiprocessors: %d\n\tGlobal memory: %zu MiB", p.multiProcessorCount,
+                (size_t)(p.totalGlobalMem >> 20));
+    std::printf("\n\tShared memory per block: %zu KiB\n\tL2 cache: %d MiB",
+                (size_t)(p.sharedMemPerBlockOptin >> 10), p.l2CacheSize >> 20);
+    std::printf("\n-----------------------------------------------------------\n");
 }
 
 void set_time(Run &r, uint64_t ti, double tf) {
@@ -209,6 +227,7 @@ void init(Run &r, const cbj::Value &in, int precision_override, int graph_overri
     if (graph_override >= 0) c.use_graph = graph_override;
     check(cb_create(&c, &r.ctx), "cb_create");
     std::printf("==============\nInitialization\n==============\n");
+    print_device();
     std::printf("bubbles %d (%d x %d x %d), box (%g, %g, %g), %s form\n", count, bpd[0], bpd[1],
                 c.dimensionality == 3 ? bpd[2] : 1, c.tfr[0], c.tfr[1], c.tfr[2],
                 c.precision ? "mixed" : "fp64");

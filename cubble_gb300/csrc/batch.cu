@@ -264,6 +264,7 @@ int batch_fail_status(cb_batch *b) {
 }
 
 int batch_integrate(cb_batch *b, int64_t n_steps, cb_report *reports, double *ms) {
+    NvtxRange nv("Batch integration");
     CB_CUDA(cudaSetDevice(b->dev));
     if (n_steps < 0) return fail(CB_ERR_INVALID_ARGUMENT, "n_steps must be >= 0");
     const int mode0 = b->first()->mode();

@@ -134,6 +134,7 @@ void launch_attempt_kernels(const cb_context *c, const Launch &l, const Bufs &b,
 namespace {
 
 int run_attempt(cb_context *c) {
+    NvtxRange nv("Integration step");
     launch_attempt_kernels(c, c->launch, c->bufs);
     return c->check_launch();
 }
@@ -154,6 +155,7 @@ int integrate_eager(cb_context *c, int64_t n_steps) {
             if (!c->hctrl->too_large) break;
         }
         if (c->hctrl->need_delete) {
+            NvtxRange nv("Removal");
             launch_remove(c->launch, c->bufs, c->hk.dim);
             int rc = c->check_launch();
             if (rc) return rc;
@@ -632,6 +634,7 @@ int cb_set_box(cb_context *c, const double lbb[3], const double tfr[3], double m
 }
 
 int cb_bootstrap(cb_context *c) {
+    NvtxRange nv("Bootstrap");
     {
         if (!c) return fail(CB_ERR_INVALID_ARGUMENT, "null context");
         CB_CUDA(cudaSetDevice(c->dev));
@@ -660,6 +663,7 @@ int cb_bootstrap(cb_context *c) {
 }
 
 int cb_search_neighbors(cb_context *c) {
+    NvtxRange nv("Neighbors");
     CB_ENTER(c);
     if (!c->loaded) return fail(CB_ERR_STATE, "state not loaded");
     int rc = run_search(c);
@@ -780,6 +784,7 @@ int cb_attempt(cb_context *c, cb_attempt_view *o) {
 }
 
 static int integrate_impl(cb_context *c, int64_t n_steps) {
+    NvtxRange nv("Integration");
     if (!c->loaded) return fail(CB_ERR_STATE, "state not loaded");
     if (n_steps < 0) return fail(CB_ERR_INVALID_ARGUMENT, "negative step count");
     int rc = c->pull();
@@ -848,6 +853,7 @@ int cb_get_report(cb_context *c, cb_report *r) {
 }
 
 int cb_energy(cb_context *c, double *out) {
+    NvtxRange nv("Energy");
     CB_ENTER(c);
     if (!out) return fail(CB_ERR_INVALID_ARGUMENT, "null output");
     launch_energy(c->launch, c->bufs, c->hk.dim, 0);
@@ -875,6 +881,7 @@ int cb_bubble_energies(cb_context *c, double *e, int32_t capacity) {
 }
 
 int cb_total_volume(cb_context *c, double *out) {
+    NvtxRange nv("Volume");
     CB_ENTER(c);
     if (!out) return fail(CB_ERR_INVALID_ARGUMENT, "null output");
     launch_volume(c->launch, c->bufs, c->hk.dim);

@@ -5,6 +5,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "common.cuh"
 
 namespace cbg {
@@ -88,6 +90,15 @@ struct cb_context {
 };
 
 namespace cbg {
+// NVTX range over a scope, named like the reference's ranges
+// (src/simulator.cu:40-376); costs nothing without a tool attached.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
 int sync_status(cb_context *c);
 int invalidate_prediction(cb_context *c);
 void launch_attempt_kernels(const cb_context *c, const Launch &l, const Bufs &b, int which = 7);

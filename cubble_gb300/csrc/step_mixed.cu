@@ -131,15 +131,21 @@ struct __align__(16) PredMx {
     float r, inv;
 };
 
+// One 32-byte load per record (a 256-bit vector load; records are 32-byte
+// aligned). Not volatile: the records are read-only while a kernel reads
+// them, so the compiler may schedule these loads freely.
 __device__ __forceinline__ PredMx ld_pred(const double *base, int i) {
-    const longlong2 *p = reinterpret_cast<const longlong2 *>(base) + 2 * (size_t)i;
-    const longlong2 u = p[0], v = p[1];
+    const long long *p = reinterpret_cast<const long long *>(base) + 4 * (size_t)i;
+    long long a, b, c, d;
+    asm("ld.global.v4.u64 {%0, %1, %2, %3}, [%4];"
+        : "=l"(a), "=l"(b), "=l"(c), "=l"(d)
+        : "l"(p));
     PredMx r;
-    r.q[0] = u.x;
-    r.q[1] = u.y;
-    r.q[2] = v.x;
-    r.r = __int_as_float((int)(v.y & 0xffffffffLL));
-    r.inv = __int_as_float((int)(v.y >> 32));
+    r.q[0] = a;
+    r.q[1] = b;
+    r.q[2] = c;
+    r.r = __int_as_float((int)(d & 0xffffffffLL));
+    r.inv = __int_as_float((int)(d >> 32));
     return r;
 }
 
