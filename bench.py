@@ -228,6 +228,28 @@ def profiled_traffic(kernel_name):
     return None
 
 
+def profiled_metric(kernel_name, label):
+    """A value of the committed ncu summary tables in profiles/ (rows
+    "| label | v1 | v2 |" under a header "| metric | kernel1 | kernel2 |"), or
+    None."""
+    import glob
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
+        cols = None
+        with open(path) as f:
+            for ln in f:
+                cells = [c.strip() for c in ln.strip().strip("|").split("|")]
+                if len(cells) > 1 and cells[0] == "metric":
+                    cols = cells[1:]
+                elif cols and len(cells) == len(cols) + 1 and cells[0] == label:
+                    if kernel_name in cols:
+                        try:
+                            return float(cells[1 + cols.index(kernel_name)].split()[0]), \
+                                os.path.relpath(path, ROOT)
+                        except ValueError:
+                            return None
+    return None
+
+
 def state_bytes(st):
     return int(sum(np.asarray(v).nbytes for v in st.values()))
 
@@ -356,6 +378,14 @@ def measure_form(args, world, rank, precision, clocks_on=True):
             "kernel_ms": dict(zip(names, kms)),
             "algorithmic_bytes_per_bubble": ab,
             "step_achieved_gbs": step_gbs, "step_frac": step_gbs / hbm}
+    fp64 = profiled_metric(kname, "FP64 pipe % active")
+    if fp64 and not precision:
+        # the FP64 form is bound by FP64 issue (2 FP64 thread-instructions per
+        # SM and cycle on GB300), not by HBM: the ncu pipe utilisation says how
+        # close the dominant kernel is to that bound
+        roof["fp64_issue_bound"] = {"pipe_active_frac": fp64[0] / 100.0,
+                                    "source": "%s (ncu sm__pipe_fp64_cycles_active of %s)"
+                                              % (fp64[1], kname)}
     sim.close()
     return {"value": bs_all / el, "el": el, "cfg": cfg, "st": st, "desc": desc, "r0": r0,
             "r1": r1, "roofline": roof, "launches": launches, "clocks": clk,

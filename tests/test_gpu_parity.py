@@ -168,6 +168,31 @@ def test_trajectory(oracle_mod, case, graph):
                                "dxdto", "error"], 1e-9, "trajectory ")
 
 
+def test_c1_full_run(oracle_mod):
+    """The 2D configuration at its stated size and length: N = 10^4, phi 0.90,
+    1000 adaptive steps with gas exchange and deletions, GPU FP64 form
+    against the oracle. Same accepted steps, attempts, searches, deletions
+    and pair count; states within 1e-8 of each row's maximum (rounding of
+    FP64 atomics over 1000 steps of a dissipative flow), total volume and
+    energy within 1e-10."""
+    import os
+    cfg, st = workloads.config_c1(use_graph=1)
+    g = cb.GpuFoam(cfg)
+    o = oracle_mod.OracleFoam(cfg, threads=os.cpu_count() or 1)
+    for f in (g, o):
+        f.load_state(st)
+        workloads.prepare(f)
+    rg, ro = g.integrate(1000), o.integrate(1000)
+    for k in ("steps", "attempts", "searches", "deleted", "count", "num_pairs"):
+        assert rg[k] == ro[k], k
+    assert rg["time_step"] == pytest.approx(ro["time_step"], rel=1e-9)
+    sg, so = by_index(g.get_state()), by_index(o.get_state())
+    assert np.array_equal(sg["index"], so["index"])
+    assert_rows_close(sg, so, ["x", "y", "r", "dxdt", "dydt", "drdt", "path"], 1e-8, "c1 ")
+    assert g.total_volume() == pytest.approx(o.total_volume(), rel=1e-10)
+    assert g.energy() == pytest.approx(o.energy(), rel=1e-10)
+
+
 @pytest.mark.parametrize("graph", [0, 1])
 @pytest.mark.parametrize("dim", [2, 3])
 def test_deletion_bit_exact_order(oracle_mod, dim, graph):
