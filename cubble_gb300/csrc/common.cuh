@@ -121,7 +121,7 @@ struct Ctrl {
     // blocks of its virtual grid in the attempt and in the search / deletion.
     int bsel, vgrid_a, vgrid_s;
     int stash_over;    // a row of the last search exceeded kStash partners
-    int sparse_cells;  // < 8 bubbles per cell: thread-per-bubble pair pass
+    int sparse_cells;  // < 24 bubbles per cell: thread-per-bubble pair pass
     // Mixed form: the correct kernel also writes the next attempt's
     // prediction for both dt it can have after an accept (unchanged, x1.269)
     // with their area sums; pred_ready says the prediction for the coming

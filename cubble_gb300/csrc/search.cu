@@ -96,7 +96,7 @@ __device__ __forceinline__ void k_wrap_body(const Bufs &b, const int vb, const i
             c->ncell = cd[0] * cd[1] * cd[2];
             c->searches += 1;
             c->stash_over = 0;
-            c->sparse_cells = (long long)c->n < 8LL * c->ncell;
+            c->sparse_cells = (long long)c->n < 24LL * c->ncell;
             c->pred_ready = 0;  // the bubbles move to new slots
             c->pred_slot = 0;
             c->done[DC_WRAP] = 0;
@@ -437,11 +437,13 @@ __device__ __forceinline__ void k_pair_cells_body(const Bufs &b, const int vb, c
 }
 CB_KERNEL_PAIR((template <int DIM, bool WRITE>), k_pair_cells, (<DIM, WRITE>), __launch_bounds__(kBlock))
 
-// Counting pass for sparse cell grids (fewer than 8 bubbles per cell on
-// average, e.g. 2D foams): one thread per bubble walks its neighbour cells
+// Counting pass for sparse cell grids (fewer than 24 bubbles per cell on
+// average: 2D foams, and 3D foams whose cell edge 2 maxR + skin holds ~10
+// bubbles): one thread per bubble walks its neighbour cells
 // >= its own cell in ascending order and the bubbles j > i in them, so the
 // rows and their order are those of the warp-per-cell pass, with all lanes
-// busy (a warp per cell of ~3 bubbles would leave 90 % of its lanes idle).
+// busy (a warp per cell of ~3 bubbles would leave 90 % of its lanes idle;
+// measured on GB300 the thread pass is faster up to at least 10 per cell).
 template <int DIM>
 __device__ __forceinline__ void k_pair_rows_body(const Bufs &b, const int vb, const int vg) {
     Ctrl *c = b.ctrl;
