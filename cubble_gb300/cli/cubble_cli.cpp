@@ -14,7 +14,8 @@
 // conditions on the device after every step).
 //
 // Extensions (not in the reference): the optional input key
-// "gb300": {"precision": "fp64" | "mixed", "graph": 0 | 1}, and the flags
+// "gb300": {"precision": "fp64" | "mixed", "graph": 0 | 1, "shear": v} (v:
+// maximum speed of a linear shear flow replacing the flow box), and the flags
 //   --precision fp64|mixed   --no-graph
 //   --checkpoint FILE        write the full state at every printed time unit
 //   --resume FILE            continue a run from such a checkpoint
@@ -222,6 +223,10 @@ void init(Run &r, const cbj::Value &in, int precision_override, int graph_overri
         const cbj::Value &g = in["gb300"];
         if (g.has("precision")) c.precision = g["precision"].string() == "mixed" ? 1 : 0;
         if (g.has("graph")) c.use_graph = g["graph"].integer() != 0;
+        // linear shear along x over the last axis instead of the flow box, in
+        // the units of flow.velocity (scaled by f0/mu0 like it); applies when
+        // flow.impose is 1
+        if (g.has("shear")) c.shear_speed = g["shear"].number() * c.f0_per_mu0;
     }
     if (precision_override >= 0) c.precision = precision_override;
     if (graph_override >= 0) c.use_graph = graph_override;

@@ -310,18 +310,18 @@ __device__ __forceinline__ void k_correct_body(const Bufs &b, const int vb, cons
         double t, dist;
         const double x0 = X[i], y0 = Y[i];
         const double cx = fma(h, V0[i] + vpx, x0);
-        e = max_bits(e, fabs(xp - cx));
+        e = max_bits(e, abs_bits(xp - cx));
         t = cx - S0[i];
         dist = t * t;
         const double cy = fma(h, V1[i] + vpy, y0);
-        e = max_bits(e, fabs(yp - cy));
+        e = max_bits(e, abs_bits(yp - cy));
         t = cy - S1[i];
         dist = fma(t, t, dist);
         double cz = 0.0, z0 = 0.0;
         if (DIM == 3) {
             z0 = Z[i];
             cz = fma(h, V2[i] + vpz, z0);
-            e = max_bits(e, fabs(zp - cz));
+            e = max_bits(e, abs_bits(zp - cz));
             t = cz - S2[i];
             dist = fma(t, t, dist);
         }
@@ -336,9 +336,9 @@ __device__ __forceinline__ void k_correct_body(const Bufs &b, const int vb, cons
             vr *= DIM == 3 ? kq * (inv * inv) : kq * inv;
             vpr = vr;
             const double cr = fma(h, V3[i] + vr, R[i]);
-            e = max_bits(e, fabs(rp - cr));
+            e = max_bits(e, abs_bits(rp - cr));
             dist += cr - S3[i];
-            if (cr > k.min_rad) {
+            if (__double_as_longlong(cr) > __double_as_longlong(k.min_rad)) {  // cr > minRad
                 vol = fma(DIM == 3 ? cr * cr : cr, cr, vol);
             } else {
                 del = 1;
@@ -362,8 +362,7 @@ __device__ __forceinline__ void k_correct_body(const Bufs &b, const int vb, cons
             }
             PATHN[i] = PATH[i] + sqrt_hn(d2);
         }
-        const double ed = __longlong_as_double(e);
-        ERR[i] = fmax(ed, ERR[i]);
+        ERR[i] = __longlong_as_double(max(e, __double_as_longlong(ERR[i])));  // both >= 0
         merr = max(merr, e);
         XN[i] = cx;
         YN[i] = cy;

@@ -87,6 +87,25 @@ def test_cli_mixed_form_and_3d(tmp_path):
     assert len(results(tmp)) >= 1
 
 
+def test_cli_walls_and_shear_3d(tmp_path):
+    """3D with walls in z and the linear shear extension (the large sheared
+    foam's setting), mixed form: runs, writes finite rows, and the mean x
+    velocity of the snapshot grows with height (the imposed profile)."""
+    tmp = str(tmp_path)
+    inp = small_input(dim=3, num=3000, **{"constants.phi.value": 0.8, "box.wall.z": 1,
+                                          "flow.impose": 1, "snapShot.frequency": 1.0})
+    inp["gb300"] = {"precision": "mixed", "shear": 0.05}
+    run_cli(tmp, ["input.json", "--max-steps", "1500"], inp)
+    rows = results(tmp)
+    assert np.all(np.isfinite(rows))
+    snaps = sorted((f for f in os.listdir(tmp) if f.startswith("bubbles.csv.")),
+                   key=lambda f: int(f.rsplit(".", 1)[1]))
+    data = np.loadtxt(os.path.join(tmp, snaps[-1]), delimiter=",", skiprows=1, ndmin=2)
+    z, vx = data[:, 2], data[:, 4]
+    lo, hi = z < np.quantile(z, 0.25), z > np.quantile(z, 0.75)
+    assert vx[hi].mean() - vx[lo].mean() > 0.02
+
+
 def test_cli_checkpoint_resume_continues(tmp_path):
     a = os.path.join(str(tmp_path), "a")
     b = os.path.join(str(tmp_path), "b")
