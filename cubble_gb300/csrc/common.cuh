@@ -294,22 +294,60 @@ __device__ __forceinline__ double fold_partials(const double *p, int nblocks, bo
 // so the FP64 kernels avoid the multi-instruction IEEE divide and square
 // root where full IEEE rounding is not needed.
 //
-// Reciprocal and reciprocal square root: the hardware's approximate FP64
-// estimate y0 (PTX rcp.approx.ftz.f64 / rsqrt.approx.f64, ~2^-22 relative)
-// refined by one third-order Householder (Newton-Raphson with the second
-// order term) correction. With e = 1 - a y0 (resp. 1 - a y0^2):
+// Reciprocal and reciprocal square root: an estimate y0 (~2^-22 relative,
+// from the FP32 unit, see rcp_seed / rsqrt_seed) refined by one third-order
+// Householder (Newton-Raphson with the second order term) correction. With
+// e = 1 - a y0 (resp. 1 - a y0^2):
 //   1/a       = y0 (1 + e + e^2 + ...)            -> error ~ e^3
 //   1/sqrt(a) = y0 (1 + e/2 + 3 e^2 / 8 + ...)    -> error ~ 5/16 e^3
 // i.e. a few ulp, for positive normal arguments. 3 and 5 FP64 instructions.
-__device__ __forceinline__ double rcp_hn(double a) {
+// Seeds from the FP32 special-function unit for positive normal doubles in
+// FP32 range: the double is truncated to FP32 and the FP32 estimate widened
+// back, both from the bit patterns on the integer pipe, so neither the
+// estimate nor the conversions take FP64 issue slots (~2^-22 relative, the
+// same quality as the FP64 approximate instructions). false when a or the
+// estimate falls outside the FP32 normal range.
+__device__ __forceinline__ bool f32_of(double a, float &f) {
+    const int hi = __double2hiint(a);
+    const unsigned int lo = (unsigned int)__double2loint(a);
+    const int fe = ((hi >> 20) & 0x7ff) - 896;
+    f = __uint_as_float(((unsigned int)fe << 23) | (((unsigned int)hi & 0xfffffu) << 3) |
+                        (lo >> 29));
+    return hi > 0 && fe > 0 && fe < 255;
+}
+__device__ __forceinline__ bool f64_of(float f, double &d) {
+    const unsigned int b = __float_as_uint(f);
+    const unsigned int e = (b >> 23) & 0xffu;
+    d = __hiloint2double((int)(((e + 896u) << 20) | ((b & 0x7fffffu) >> 3)), (int)((b & 7u) << 29));
+    return e > 0 && e < 255 && !(b >> 31);
+}
+__device__ __forceinline__ double rcp_seed(double a) {
+    float f, r;
     double y;
+    if (f32_of(a, f)) {
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(f));
+        if (f64_of(r, y)) return y;
+    }
     asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(a));
+    return y;
+}
+__device__ __forceinline__ double rsqrt_seed(double a) {
+    float f, r;
+    double y;
+    if (f32_of(a, f)) {
+        asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(f));
+        if (f64_of(r, y)) return y;
+    }
+    asm("rsqrt.approx.f64 %0, %1;" : "=d"(y) : "d"(a));
+    return y;
+}
+__device__ __forceinline__ double rcp_hn(double a) {
+    const double y = rcp_seed(a);
     const double e = fma(-a, y, 1.0);
     return fma(y, fma(e, e, e), y);
 }
 __device__ __forceinline__ double rsqrt_hn(double a) {
-    double y;
-    asm("rsqrt.approx.f64 %0, %1;" : "=d"(y) : "d"(a));
+    const double y = rsqrt_seed(a);
     const double t = a * y;
     const double e = fma(-t, y, 1.0);
     return fma(y * e, fma(e, 0.375, 0.5), y);
