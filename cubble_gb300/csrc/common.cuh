@@ -151,7 +151,7 @@ struct Bufs {
     int *const *ps;     // pair slots
     double *pred;       // 4 doubles per bubble
     double *predc;      // mixed form: two candidate predictions, 8 doubles per bubble
-    double *invr;       // 1 / rp (3D)
+    double *invr;       // FP64 form, 3D: (1 / rp, rp^2) per bubble
     double *acc;        // kAcc doubles per bubble
     double *part;       // kPartSlots x grid partials
     int *delflag;       // deletion marks of the last attempt
@@ -371,6 +371,19 @@ __device__ __forceinline__ bool less_nonneg(double a, double b) {
 }
 __device__ __forceinline__ double min_nonneg(double a, double b) {
     return __longlong_as_double(min(__double_as_longlong(a), __double_as_longlong(b)));
+}
+
+// Second-order variant (one Newton step, ~2^-44 relative): for square roots
+// whose result is only summed or compared (path increments, expansion), two
+// FP64 instructions fewer.
+__device__ __forceinline__ double rsqrt_hn2(double a) {
+    const double y = rsqrt_seed(a);
+    const double t = a * y;
+    const double e = fma(-t, y, 1.0);
+    return fma(0.5 * y, e, y);
+}
+__device__ __forceinline__ double sqrt_hn2(double a) {
+    return __double_as_longlong(a) > 0 ? a * rsqrt_hn2(a) : 0.0;
 }
 
 // sqrt(a) = a / sqrt(a) for a > 0, 0 for a <= 0.

@@ -375,7 +375,7 @@ int cb_create(const cb_config *cfg, cb_context **out) {
     if ((rc = c->alloc(&c->d_pslots, NP_ROLES))) return bail(rc);
     if ((rc = c->alloc(&b.pred, 4 * cap))) return bail(rc);
     if (c->hk.mixed && (rc = c->alloc(&b.predc, 8 * cap))) return bail(rc);
-    if ((rc = c->alloc(&b.invr, cap))) return bail(rc);
+    if ((rc = c->alloc(&b.invr, 2 * cap))) return bail(rc);
     if ((rc = c->alloc(&b.acc, (size_t)kAcc * cap))) return bail(rc);
     if ((rc = c->alloc(&b.part, (size_t)kPartSlots * G))) return bail(rc);
     if ((rc = c->alloc(&b.delflag, cap + 1))) return bail(rc);

@@ -51,7 +51,7 @@ __device__ __forceinline__ void k_predict_body(const Bufs &b, const int vb, cons
             p.y = yp;
             p.z = fma(h, fma(3.0, V2[i], -O2[i]), Z[i]);
             p.w = rp;
-            b.invr[i] = inv;
+            reinterpret_cast<double2 *>(b.invr)[i] = make_double2(inv, rp * rp);
         } else {
             p.x = xp;
             p.y = yp;
@@ -143,27 +143,35 @@ __device__ __forceinline__ void k_pairs_body(const Bufs &b, const int vb, const 
                 atomicAdd(aj + 2, neg_bits(fz));
             }
             if (GAS) {  // pairwise gas exchange, src/kernels.cu:236-280
-                const double r1sq = r1 * r1, r2sq = r2 * r2;
+                // 3D: (1/r, r^2) records written by k_predict
+                double2 e1 = make_double2(0.0, 0.0), e2 = e1;
+                if (DIM == 3) {
+                    e1 = reinterpret_cast<const double2 *>(b.invr)[i];
+                    e2 = reinterpret_cast<const double2 *>(b.invr)[j];
+                }
+                const double r1sq = DIM == 3 ? e1.y : r1 * r1, r2sq = DIM == 3 ? e2.y : r2 * r2;
                 const bool inside = less_nonneg(m, r1sq) || less_nonneg(m, r2sq);
+                // chord: r2^2 - t^2 / m with t = (r2^2 - r1^2 + m) / 2, as
+                // r2^2 - w^2 / 4 with w = (r2^2 - r1^2 + m) / |d|
                 double oa;
                 if (DIM == 3) {
                     if (inside) {
                         oa = min_nonneg(r1sq, r2sq);
                     } else {
-                        const double t = 0.5 * (r2sq - r1sq + m);
-                        oa = abs_bits(r2sq - (t * t) * (rs * rs));
+                        const double w = (r2sq - r1sq + m) * rs;
+                        oa = abs_bits(fma(-0.25 * w, w, r2sq));
                     }
                     oa *= kPi;
                 } else {
                     if (inside) {
                         oa = 2.0 * min_nonneg(r1, r2);
                     } else {
-                        const double t = 0.5 * (r2sq - r1sq + m);
-                        oa = 2.0 * sqrt_hn(abs_bits(r2sq - (t * t) * (rs * rs)));
+                        const double w = (r2sq - r1sq + m) * rs;
+                        oa = 2.0 * sqrt_hn(abs_bits(fma(-0.25 * w, w, r2sq)));
                     }
                 }
-                const double inv1 = DIM == 3 ? b.invr[i] : a.w;
-                const double inv2 = DIM == 3 ? b.invr[j] : q.w;
+                const double inv1 = DIM == 3 ? e1.x : a.w;
+                const double inv2 = DIM == 3 ? e2.x : q.w;
                 const double g = oa * (inv2 - inv1);
                 atomicAdd(ai + 3, g);
                 atomicAdd(aj + 3, neg_bits(g));
@@ -325,10 +333,10 @@ __device__ __forceinline__ void k_correct_body(const Bufs &b, const int vb, cons
             t = cz - S2[i];
             dist = fma(t, t, dist);
         }
-        dist = sqrt_hn(dist);
+        dist = sqrt_hn2(dist);  // only its maximum over the foam is used
         int del = 0;
         if (gas) {  // mean-field gas exchange and radius, src/kernels.cu:390-431
-            const double inv = DIM == 3 ? b.invr[i] : p.w;
+            const double inv = DIM == 3 ? b.invr[2 * (size_t)i] : p.w;
             const double area = DIM == 3 ? (4.0 * kPi) * (rp * rp) : (2.0 * kPi) * rp;
             double vr = mfa - inv;
             vr *= mfb * (area - ov);
@@ -360,7 +368,7 @@ __device__ __forceinline__ void k_correct_body(const Bufs &b, const int vb, cons
                 t = z0 - cz;
                 d2 = fma(t, t, d2);
             }
-            PATHN[i] = PATH[i] + sqrt_hn(d2);
+            PATHN[i] = PATH[i] + sqrt_hn2(d2);  // ~1e-13 relative per increment
         }
         ERR[i] = __longlong_as_double(max(e, __double_as_longlong(ERR[i])));  // both >= 0
         merr = max(merr, e);
@@ -433,7 +441,7 @@ __global__ void __launch_bounds__(kBlock) k_boot(Bufs b, int phase) {
             if (DIM == 3) {
                 p.z = Z[i];
                 p.w = r;
-                b.invr[i] = 1.0 / r;
+                reinterpret_cast<double2 *>(b.invr)[i] = make_double2(1.0 / r, r * r);
             } else {
                 p.z = r;
                 p.w = 1.0 / r;
