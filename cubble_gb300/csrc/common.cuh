@@ -122,6 +122,7 @@ struct Ctrl {
     int bsel, vgrid_a, vgrid_s;
     int stash_over;    // a row of the last search exceeded kStash partners
     int sparse_cells;  // < 24 bubbles per cell: thread-per-bubble pair pass
+    float search_maxr;  // the search's largest radius, rounded up to FP32
     // Mixed form: the correct kernel also writes the next attempt's
     // prediction for both dt it can have after an accept (unchanged, x1.269)
     // with their area sums; pred_ready says the prediction for the coming

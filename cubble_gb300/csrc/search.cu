@@ -97,6 +97,7 @@ __device__ __forceinline__ void k_wrap_body(const Bufs &b, const int vb, const i
             c->searches += 1;
             c->stash_over = 0;
             c->sparse_cells = (long long)c->n < 24LL * c->ncell;
+            c->search_maxr = __double2float_ru(f);
             c->pred_ready = 0;  // the bubbles move to new slots
             c->pred_slot = 0;
             c->done[DC_WRAP] = 0;
@@ -456,31 +457,77 @@ __device__ __forceinline__ void k_pair_rows_body(const Bufs &b, const int vb, co
     const double *X = drow(b, c, RX), *Y = drow(b, c, RY), *Z = drow(b, c, RZ),
                  *R = drow(b, c, RR);
     int *NN = irow(b, c, INN);
+    // cell widths and the reach beyond a bubble's radius (FP32, padded so the
+    // cell pruning below never drops a partner)
+    float cw[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) cw[a] = k.iv32[a] / (float)cd[a];
+    const float reach0 = c->search_maxr + (float)k.skin + k.pre_margin + 1e-3f;
     bool over = false;
     for (int i = vb * blockDim.x + threadIdx.x; i < n; i += vg * blockDim.x) {
         const int cell = b.cellSorted[i];
+        const int kk[3] = {cell % cd[0], (cell / cd[0]) % cd[1], cell / (cd[0] * cd[1])};
+        const float4 pi = b.pos32[i];
+        const float pr[3] = {pi.x - (float)k.lbb[0], pi.y - (float)k.lbb[1],
+                             DIM == 3 ? pi.z - (float)k.lbb[2] : 0.f};
+        const float reach = pi.w + reach0;
+        // distance from the bubble to the lower / upper face of its cell
+        float lo[3], hi[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            lo[a] = fmaxf(pr[a] - (float)kk[a] * cw[a], 0.f);
+            hi[a] = fmaxf((float)(kk[a] + 1) * cw[a] - pr[a], 0.f);
+        }
         int nb[NO];
         int nq = 0;
 #pragma unroll
         for (int t = 0; t < NO; t++) {
             const int o = DIM == 3 ? t : 9 + t;  // 2D: the z-offset-0 plane
-            const int v = neighbor_cell<DIM>(k, cd, cell, o);
-            if (v != 0x7fffffff) {
-                int p = nq++;  // insertion into the ascending list
-                while (p > 0 && nb[p - 1] > v) {
-                    nb[p] = nb[p - 1];
-                    p--;
+            const int off[3] = {o % 3 - 1, (o / 3) % 3 - 1, o / 9 - 1};
+            // neighbour cell index (getNeighborCellIndex, src/kernels.cu:1157-1189)
+            int q[3];
+            bool ok = true;
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                const int d = cd[a];
+                if (a >= DIM) {
+                    ok &= off[a] == 0;
+                    q[a] = 0;
+                } else if (!k.wall[a]) {
+                    ok &= !(d == 1 && off[a] != 0) && !(d == 2 && off[a] == -1);
+                    q[a] = kk[a] + off[a];
+                    q[a] = q[a] < 0 ? q[a] + d : (q[a] >= d ? q[a] - d : q[a]);
+                } else {
+                    q[a] = kk[a] + off[a];
+                    ok &= q[a] >= 0 && q[a] < d;
                 }
-                nb[p] = v;
             }
+            const int v = (q[2] * cd[1] + q[1]) * cd[0] + q[0];
+            if (!ok || v < cell) continue;
+            // skip a neighbour cell no partner of this bubble can be in
+            float d2 = 0.f;
+#pragma unroll
+            for (int a = 0; a < DIM; a++) {
+                // with two cells on a periodic axis the other cell touches
+                // both faces (only its +1 offset is enumerated)
+                const float up = (!k.wall[a] && cd[a] == 2) ? fminf(lo[a], hi[a]) : hi[a];
+                const float f = off[a] > 0 ? up : (off[a] < 0 ? lo[a] : 0.f);
+                d2 = fmaf(f, f, d2);
+            }
+            if (d2 > reach * reach) continue;
+            int p = nq++;  // insertion into the ascending list
+            while (p > 0 && nb[p - 1] > v) {
+                nb[p] = nb[p - 1];
+                p--;
+            }
+            nb[p] = v;
         }
-        const float4 pi = b.pos32[i];
         double xi = 0.0, yi = 0.0, zi = 0.0, ri = 0.0;
         int cnt = 0;
         for (int t = 0; t < nq; t++) {
-            const int q = nb[t];
-            const int ce = b.cellStart[q + 1];
-            for (int j = max(b.cellStart[q], i + 1); j < ce; j++) {
+            const int qc = nb[t];
+            const int ce = b.cellStart[qc + 1];
+            for (int j = max(b.cellStart[qc], i + 1); j < ce; j++) {
                 if (pair_take<DIM>(k, pi, b.pos32[j], i, j, X, Y, Z, R, xi, yi, zi, ri)) {
                     if (cnt < M) b.stash[(size_t)i * M + cnt] = j;
                     cnt++;
