@@ -327,6 +327,14 @@ int cb_create(const cb_config *cfg, cb_context **out) {
     if (cfg->capacity <= 0) return fail(CB_ERR_INVALID_ARGUMENT, "capacity must be positive");
     if ((long long)cfg->capacity * 2 + 64 > 0x7fffffffLL)
         return fail(CB_ERR_INVALID_ARGUMENT, "capacity too large");
+    {  // pair-list offsets are int32 (row starts, the pair count)
+        const long long pcap = cfg->pair_capacity > 0
+                                   ? (long long)cfg->pair_capacity
+                                   : (long long)(cfg->dimensionality == 3 ? 16 : 8) * cfg->capacity;
+        if (cfg->pair_capacity < 0 || pcap + 1 > 0x7fffffffLL)
+            return fail(CB_ERR_INVALID_ARGUMENT,
+                        "pair capacity beyond 2^31 - 2 (set pair_capacity or lower capacity)");
+    }
     if (cfg->precision == CB_PRECISION_MIXED) {
         for (int a = 0; a < 3; a++)
             if (std::fabs(cfg->lbb[a]) > 2097152.0 || std::fabs(cfg->tfr[a]) > 2097152.0)

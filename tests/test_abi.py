@@ -77,6 +77,27 @@ def test_invalid_configuration_is_rejected(gpu_lib):
     assert e.value.code in (_abi.CB_ERR_INVALID_ARGUMENT, _abi.CB_ERR_NO_DEVICE)
 
 
+@pytest.mark.parametrize("dim,capacity,pair_capacity,ok", [
+    (3, 134_000_000, 0, True),         # default 16 per bubble: 2.14e9 pairs
+    (3, 135_000_000, 0, False),        # default would pass 2^31 - 2
+    (3, 135_000_000, 1_500_000_000, True),
+    (2, 268_000_000, 0, True),         # default 8 per bubble in 2D
+    (2, 10, -1, False),
+    (2, 10, 2_147_483_647, False),
+])
+def test_pair_capacity_range(gpu_lib, dim, capacity, pair_capacity, ok):
+    """Configuration checks run before the device is touched: a pair list
+    that int32 offsets cannot address is rejected on any machine."""
+    import torch
+    cfg = cb.make_config(dimensionality=dim, capacity=capacity, pair_capacity=pair_capacity)
+    if ok and torch.cuda.is_available():
+        pytest.skip("would allocate the full capacity")
+    with pytest.raises(CubbleError) as e:
+        cb.GpuFoam(cfg)
+    want = _abi.CB_ERR_NO_DEVICE if ok else _abi.CB_ERR_INVALID_ARGUMENT
+    assert e.value.code == want, cb.lib().cb_last_error()
+
+
 def test_no_device_fails_loudly(gpu_lib):
     """With no GPU the product raises; it never computes on the CPU."""
     import torch
