@@ -188,7 +188,7 @@ def allreduce(x, op, world):
     return float(t.item())
 
 
-def algorithmic_bytes(dim, np_per_n, mixed=False):
+def algorithmic_bytes(dim, np_per_n, mixed=False, ff=False):
     """Algorithmic HBM bytes per bubble of each attempt kernel.
 
     FP64 form, 3D: predict reads x,y,z,r, v x4, v_old x4 (96) and writes the
@@ -200,7 +200,15 @@ def algorithmic_bytes(dim, np_per_n, mixed=False):
     Mixed form (FP32 rates, 32-byte fixed-point prediction, 20-byte FP32
     accumulators), 3D: predict 64 + 32, pairs 8 P/N + 32 + 20, correct
     132 + 88; step 176 + 8 P/N (q FP64 r/w 64, f FP32 r/w 32, f_old 16,
-    saved 32, path 16, error 16)."""
+    saved 32, path 16, error 16). The float-float form (CB_PRECISION_FP64_FF)
+    adds its 32-byte per-bubble records: written by predict, read by pairs
+    (which reads them instead of the 16-byte (1/r, r^2) row in 3D); the
+    step's compulsory traffic is the FP64 form's."""
+    if ff:
+        b = algorithmic_bytes(dim, np_per_n)
+        b["predict"] += 32.0
+        b["pairs"] += 32.0 - (16.0 if dim == 3 else 0.0)
+        return b
     if mixed:
         if dim == 3:
             return {"predict": 96.0, "pairs": 52.0 + 8.0 * np_per_n, "correct": 220.0,
@@ -353,7 +361,8 @@ def measure_form(args, world, rank, precision, clocks_on=True):
     kms = sim.profile_kernels(reps=5)
     names = ["predict", "pairs", "correct"]
     top = int(np.argmax(kms))
-    ab = algorithmic_bytes(dim, np_per_n, mixed=bool(precision))
+    mixed = precision == 1
+    ab = algorithmic_bytes(dim, np_per_n, mixed=mixed, ff=precision == 2)
     n_now = r1["count"]
     hbm, src = peaks()
     achieved = ab[names[top]] * n_now / (kms[top] * 1e-3) / 1e9
@@ -361,12 +370,14 @@ def measure_form(args, world, rank, precision, clocks_on=True):
     # of a speculated prediction included): algorithmic bytes x measured rate
     step_gbs = ab["step"] * (bs_all / el) / 1e9
     gas, flow = int(cfg.use_gas_exchange), int(cfg.use_flow)
-    sfx = "_mx" if precision else ""
+    sfx = "_mx" if mixed else ""
     walls = int(any(cfg.wall[:dim]))
-    kcorr = ("k_correct_mx<%d, %d, %d, %d>" % (dim, gas, flow, walls) if precision
+    kcorr = ("k_correct_mx<%d, %d, %d, %d>" % (dim, gas, flow, walls) if mixed
              else "k_correct<%d>" % dim)
+    kpairs = "k_pairs%s<%d, %d, %d>" % (sfx if mixed else ("_ff" if precision == 2 else ""),
+                                        dim, gas, flow)
     kname = {"predict": "k_predict%s<%d>" % (sfx, dim), "correct": kcorr,
-             "pairs": "k_pairs%s<%d, %d, %d>" % (sfx, dim, gas, flow)}[names[top]]
+             "pairs": kpairs}[names[top]]
     tr = profiled_traffic(kname)
     roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": hbm,
             "unit": "GB/s", "frac": achieved / hbm,
@@ -379,7 +390,7 @@ def measure_form(args, world, rank, precision, clocks_on=True):
             "algorithmic_bytes_per_bubble": ab,
             "step_achieved_gbs": step_gbs, "step_frac": step_gbs / hbm}
     fp64 = profiled_metric(kname, "FP64 pipe % active")
-    if fp64 and not precision:
+    if fp64 and precision == 0:
         # the FP64 form is bound by FP64 issue (2 FP64 thread-instructions per
         # SM and cycle on GB300), not by HBM: the ncu pipe utilisation says how
         # close the dominant kernel is to that bound
@@ -392,14 +403,15 @@ def measure_form(args, world, rank, precision, clocks_on=True):
             "np_per_n": np_per_n}
 
 
-def mixed_errors(args, steps=50):
-    """Per-quantity error of the mixed form against the FP64 form (which
-    matches the FP64 oracle within 1e-12 per step) from the same prepared
-    state: one attempt, then `steps` accepted steps."""
+def form_errors(args, precision=1, steps=50):
+    """Per-quantity error of another form (mixed, or the float-float FP64
+    form) against the FP64 form (which matches the FP64 oracle within 1e-12
+    per step) from the same prepared state: one attempt, then `steps`
+    accepted steps."""
     import cubble_gb300 as cb
     from cubble_gb300 import workloads
     cfg64, st, _ = workload(args.workload, args.seed, precision=0, use_graph=1)
-    cfgmx, _, _ = workload(args.workload, args.seed, precision=1, use_graph=1)
+    cfgmx, _, _ = workload(args.workload, args.seed, precision=precision, use_graph=1)
     a = cb.GpuFoam(cfg64)
     a.load_state(st)
     workloads.prepare(a)
@@ -414,10 +426,13 @@ def mixed_errors(args, steps=50):
 
     def rel(x, y):
         return float(np.max(np.abs(x - y)) / max(np.max(np.abs(y)), 1e-300))
+    def ulps(x, y):  # largest difference in units in the last place of y
+        return float(np.max(np.abs(x - y) / np.spacing(np.maximum(np.abs(y), 1e-300))))
     aa, ab_ = a.attempt(), b.attempt()
     out = {"attempt": {}}
     for k, base in (("xp", "x"), ("yp", "y"), ("zp", "z"), ("rp", "r")):
         out["attempt"]["d" + base] = rel(ab_[k] - s0[base], aa[k] - s0[base])
+        out["attempt"][base + "_ulps"] = ulps(ab_[k], aa[k])
     for k in ("dxdtp", "dydtp", "dzdtp", "drdtp", "overlap"):
         out["attempt"][k] = rel(ab_[k], aa[k])
     for k in ("total_area", "total_overlap_area", "total_overlap_area_per_radius"):
@@ -436,13 +451,17 @@ def mixed_errors(args, steps=50):
                 ra[k] - ra0[k] == rb[k] - rb0[k] for k in ("attempts", "searches", "deleted"))}
     for k in ("x", "y", "z"):
         traj["d" + k] = rel(sb[k][ob_] - s0[k][o0], sa[k][oa_] - s0[k][o0])
+        traj[k + "_ulps"] = ulps(sb[k][ob_], sa[k][oa_])
     traj["r"] = rel(sb["r"][ob_], sa["r"][oa_])
     traj["volume_drift"] = abs(b.total_volume() / a.total_volume() - 1.0)
     traj["volume_change_fp64"] = a.total_volume() / v0 - 1.0
     traj["energy"] = abs(b.energy() / a.energy() - 1.0)
     out["trajectory"] = traj
     out["reference"] = "the FP64 form of this library on the same input (equal to the FP64 oracle within 1e-12 per step)"
-    out["error_definition"] = "max over bubbles |mixed - fp64| / max |fp64| per row (positions, radii: their change)"
+    out["error_definition"] = ("max over bubbles |form - fp64| / max |fp64| per row (positions, "
+                               "radii: their change over the attempt or the run, which can be "
+                               "a few 1e-6 at small dt); *_ulps: the largest difference in "
+                               "units in the last place of the FP64 value")
     a.close()
     b.close()
     return out
@@ -611,7 +630,23 @@ def run_gb300(args, world, rank, local):
                              "fixed-point differences, FP32 rates; FP64 positions, radii, "
                              "volume sum and fix, error norm, energy"}
         if rank == 0:
-            mixed["error_vs_fp64"] = mixed_errors(args)
+            mixed["error_vs_fp64"] = form_errors(args, 1)
+
+    fp64_ff = None
+    if args.precision == 0 and not args.no_ff:
+        fx = measure_form(args, world, rank, 2, clocks_on=False)
+        fp64_ff = {"value": fx["value"], "unit": "bubble-steps/s",
+                   "ms_per_step": 1e3 * fx["el"] / args.steps,
+                   "speedup_vs_fp64": fx["value"] / value,
+                   "attempts": fx["r1"]["attempts"] - fx["r0"]["attempts"],
+                   "searches": fx["r1"]["searches"] - fx["r0"]["searches"],
+                   "roofline": fx["roofline"], "gpu_launches": fx["launches"],
+                   "dtype": "f64 state and update; pair terms in float-float (2 x f32)",
+                   "workload": "same foam, CB_PRECISION_FP64_FF: the FP64 form with the pair "
+                               "kernel's distance, velocities, gas flux and overlap areas in "
+                               "float-float (~2^-46 relative) on the FP32 pipe"}
+        if rank == 0:
+            fp64_ff["error_vs_fp64"] = form_errors(args, 2)
 
     batched = None
     if not args.no_batch:
@@ -629,9 +664,11 @@ def run_gb300(args, world, rank, local):
         "metric": METRIC, "value": value, "unit": "bubble-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == 0 else "f64/f32 mixed",
+        "dtype": {0: "f64", 1: "f64/f32 mixed", 2: "f64 + float-float (2 x f32) pair terms"}[
+            args.precision],
         "data": "synthetic (seeded, uniform positions)",
-        "config": {"workload": desc, "precision": "fp64" if args.precision == 0 else "mixed",
+        "config": {"workload": desc,
+                   "precision": {0: "fp64", 1: "mixed", 2: "fp64_ff"}[args.precision],
                    "graph": bool(args.graph), "parallelism": "replicas" if world > 1 else "single foam",
                    "l2": "working set larger than L2 (state + pairs > 129 MB)",
                    "attempts": attempts, "searches": searches,
@@ -639,7 +676,7 @@ def run_gb300(args, world, rank, local):
                    "deleted": r1["deleted"] - r0["deleted"], "dt_end": r1["time_step"]},
         "roofline": main["roofline"], "cpu_baseline": base, "e2e": e2e,
         "gpu_launches": main["launches"], "clocks": main["clocks"], "mixed": mixed,
-        "batched": batched,
+        "fp64_ff": fp64_ff, "batched": batched,
     }
     print(json.dumps(line))
 
@@ -667,6 +704,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-ff", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--until-deleted", type=float, default=0.0)
     ap.add_argument("--chunk-steps", type=int, default=2000)

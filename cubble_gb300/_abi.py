@@ -23,6 +23,7 @@ CB_ERR_STATE = 8
 
 CB_PRECISION_FP64 = 0
 CB_PRECISION_MIXED = 1
+CB_PRECISION_FP64_FF = 2
 
 STATUS_NAMES = {
     0: "ok", 1: "invalid argument", 2: "cuda error", 3: "capacity exceeded",

@@ -14,9 +14,9 @@
 // conditions on the device after every step).
 //
 // Extensions (not in the reference): the optional input key
-// "gb300": {"precision": "fp64" | "mixed", "graph": 0 | 1, "shear": v} (v:
+// "gb300": {"precision": "fp64" | "mixed" | "fp64_ff", "graph": 0 | 1, "shear": v} (v:
 // maximum speed of a linear shear flow replacing the flow box), and the flags
-//   --precision fp64|mixed   --no-graph
+//   --precision fp64|mixed|fp64_ff   --no-graph
 //   --checkpoint FILE        write the full state at every printed time unit
 //   --resume FILE            continue a run from such a checkpoint
 //   --max-steps N            stop after N integration steps (testing)
@@ -149,6 +149,15 @@ void set_time(Run &r, uint64_t ti, double tf) {
 }
 
 // ------------------------------------------------------------------ init()
+int precision_code(const std::string &name) {
+    if (name == "mixed") return CB_PRECISION_MIXED;
+    if (name == "fp64_ff") return CB_PRECISION_FP64_FF;
+    return CB_PRECISION_FP64;
+}
+const char *precision_name(int p) {
+    return p == CB_PRECISION_MIXED ? "mixed" : p == CB_PRECISION_FP64_FF ? "fp64_ff" : "fp64";
+}
+
 void init(Run &r, const cbj::Value &in, int precision_override, int graph_override) {
     const cbj::Value &constants = in["constants"], &bubbles = in["bubbles"], &box = in["box"];
     const cbj::Value &wall = box["wall"], &flow = in["flow"];
@@ -221,7 +230,7 @@ void init(Run &r, const cbj::Value &in, int precision_override, int graph_overri
     c.use_graph = 1;
     if (in.has("gb300")) {
         const cbj::Value &g = in["gb300"];
-        if (g.has("precision")) c.precision = g["precision"].string() == "mixed" ? 1 : 0;
+        if (g.has("precision")) c.precision = precision_code(g["precision"].string());
         if (g.has("graph")) c.use_graph = g["graph"].integer() != 0;
         // linear shear along x over the last axis instead of the flow box, in
         // the units of flow.velocity (scaled by f0/mu0 like it); applies when
@@ -235,7 +244,7 @@ void init(Run &r, const cbj::Value &in, int precision_override, int graph_overri
     print_device();
     std::printf("bubbles %d (%d x %d x %d), box (%g, %g, %g), %s form\n", count, bpd[0], bpd[1],
                 c.dimensionality == 3 ? bpd[2] : 1, c.tfr[0], c.tfr[1], c.tfr[2],
-                c.precision ? "mixed" : "fp64");
+                precision_name(c.precision));
 
     // starting data: the reference's cuRAND MTGP32 draws in its order
     // (src/simulator.cu:676-692); the normal draw needs an even length
@@ -762,7 +771,7 @@ int main(int argc, char **argv) {
         try {
             if (s == "--precision") {
                 const std::string v = next();
-                precision = v == "mixed" ? CB_PRECISION_MIXED : CB_PRECISION_FP64;
+                precision = precision_code(v);
             } else if (s == "--no-graph") {
                 graph = 0;
             } else if (s == "--checkpoint") {

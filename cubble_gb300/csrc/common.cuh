@@ -21,6 +21,7 @@
 #include <stdint.h>
 
 #include "../../include/cubble_gb300.h"
+#include "ff.cuh"
 
 namespace cbg {
 
@@ -74,6 +75,8 @@ struct DevConst {
     long long lq[3], hq[3];
     int mixed;
     float f0_f;  // f0/mu0 as FP32
+    float f0_l;  // f0/mu0 - f0_f: the float-float f0 of k_pairs_ff
+    int ffpair;  // CB_PRECISION_FP64_FF: pair terms in float-float
     float kq_f;  // K / (4 pi) in 3D, K / (2 pi) in 2D, as FP32
     float pre_margin;  // FP32 pair-search prefilter margin (length units)
     float half_iv32[3];
@@ -153,6 +156,7 @@ struct Bufs {
     double *pred;       // 4 doubles per bubble
     double *predc;      // mixed form: two candidate predictions, 8 doubles per bubble
     double *invr;       // FP64 form, 3D: (1 / rp, rp^2) per bubble
+    float4 *ffr;        // CB_PRECISION_FP64_FF: float-float (rp, 1 / rp), (rp^2, 0)
     double *acc;        // kAcc doubles per bubble
     double *part;       // kPartSlots x grid partials
     int *delflag;       // deletion marks of the last attempt
@@ -642,7 +646,8 @@ inline int wave_grid(K kernel, const Launch &l) {
 
 // step.cu
 void launch_predict(const Launch &l, const Bufs &b, int dim);
-void launch_pairs(const Launch &l, const Bufs &b, int dim, int mode);  // mode: 0 step, 1 bootstrap
+void launch_pairs(const Launch &l, const Bufs &b, int dim, int mode,
+                  bool ff);  // mode: gas 1 | flow 2; ff: float-float kernel
 void launch_correct(const Launch &l, const Bufs &b, int dim);
 void launch_boot(const Launch &l, const Bufs &b, int dim, int phase);
 // step_mixed.cu (mixed form)

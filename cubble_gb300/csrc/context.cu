@@ -77,7 +77,9 @@ void fill_const(cb_context *c) {
         k.iv32[a] = (float)k.iv[a];
     }
     k.mixed = f.precision == CB_PRECISION_MIXED ? 1 : 0;
+    k.ffpair = f.precision == CB_PRECISION_FP64_FF ? 1 : 0;
     k.f0_f = (float)k.f0;
+    k.f0_l = (float)(k.f0 - (double)k.f0_f);
     k.kq_f = (float)(k.dim == 3 ? k.K / (4.0 * 3.1415926535897932384626433832795) :
                                   k.K / (2.0 * 3.1415926535897932384626433832795));
     for (int a = 0; a < 3; a++) {
@@ -124,7 +126,7 @@ void launch_attempt_kernels(const cb_context *c, const Launch &l, const Bufs &b,
         if (which & 4) launch_correct_mx(l, b, dim, c->mode(), c->hk.any_wall != 0);
     } else {
         if (which & 1) launch_predict(l, b, dim);
-        if (which & 2) launch_pairs(l, b, dim, c->mode());
+        if (which & 2) launch_pairs(l, b, dim, c->mode(), c->hk.ffpair != 0);
         if (which & 4) launch_correct(l, b, dim);
     }
 }
@@ -335,6 +337,9 @@ int cb_create(const cb_config *cfg, cb_context **out) {
             return fail(CB_ERR_INVALID_ARGUMENT,
                         "pair capacity beyond 2^31 - 2 (set pair_capacity or lower capacity)");
     }
+    if (cfg->precision != CB_PRECISION_FP64 && cfg->precision != CB_PRECISION_MIXED &&
+        cfg->precision != CB_PRECISION_FP64_FF)
+        return fail(CB_ERR_INVALID_ARGUMENT, "unknown precision");
     if (cfg->precision == CB_PRECISION_MIXED) {
         for (int a = 0; a < 3; a++)
             if (std::fabs(cfg->lbb[a]) > 2097152.0 || std::fabs(cfg->tfr[a]) > 2097152.0)
@@ -384,6 +389,7 @@ int cb_create(const cb_config *cfg, cb_context **out) {
     if ((rc = c->alloc(&b.pred, 4 * cap))) return bail(rc);
     if (c->hk.mixed && (rc = c->alloc(&b.predc, 8 * cap))) return bail(rc);
     if ((rc = c->alloc(&b.invr, 2 * cap))) return bail(rc);
+    if (c->hk.ffpair && (rc = c->alloc(&b.ffr, 2 * cap))) return bail(rc);
     if ((rc = c->alloc(&b.acc, (size_t)kAcc * cap))) return bail(rc);
     if ((rc = c->alloc(&b.part, (size_t)kPartSlots * G))) return bail(rc);
     if ((rc = c->alloc(&b.delflag, cap + 1))) return bail(rc);
@@ -660,9 +666,9 @@ int cb_bootstrap(cb_context *c) {
         launch_boot_mx(c->launch, c->bufs, dim, 2);
     } else {
         launch_boot(c->launch, c->bufs, dim, 0);
-        launch_pairs(c->launch, c->bufs, dim, 0);
+        launch_pairs(c->launch, c->bufs, dim, 0, c->hk.ffpair != 0);
         launch_boot(c->launch, c->bufs, dim, 1);
-        launch_pairs(c->launch, c->bufs, dim, 0);
+        launch_pairs(c->launch, c->bufs, dim, 0, c->hk.ffpair != 0);
         launch_boot(c->launch, c->bufs, dim, 2);
     }
     int rc = c->check_launch();

@@ -1,0 +1,314 @@
+// Float-float ("double-FP32") arithmetic for the FP64 form's pair kernel.
+//
+// GB300 issues FP64 at 1/64 of the FP32 rate, so the pair geometry, the
+// overlap velocities and the gas-exchange terms of the FP64 form are carried
+// as unevaluated sums h + l of two floats (about 47 significant bits, relative
+// error per operation ~2^-46) on the FP32 and integer pipes. Only the
+// position differences stay FP64 instructions (the reference's
+// wrappedDifference, src/kernels.cu:1094-1114).
+//
+// Methods (all from the published literature, written here from the maths):
+//   * error-free transformations: Knuth's TwoSum, Dekker's Fast2Sum, and the
+//     FMA product error a*b - fl(a*b) (Dekker / Kahan);
+//   * double-word sums and products: the "sloppy" sum and the FMA product of
+//     Joldes, Muller and Popescu, "Tight and rigorous error bounds for basic
+//     building blocks of double-word arithmetic", ACM TOMS 44 (2017);
+//   * reciprocal and reciprocal square root: an FP32 estimate, one FP32 Newton
+//     step, then one correction from the residual e = 1 - a y (resp. 1 - a y^2)
+//     evaluated in double-word: 1/a = y (1 + e + e^2), 1/sqrt(a) = y (1 + e/2 +
+//     3 e^2 / 8).
+// Conversions between double and float-float are done on the bit patterns
+// (integer pipe), so they take no FP64 issue slot.
+//
+// Functions are __host__ __device__ so the CPU tests evaluate the same code;
+// on the host the FP32 estimates come from IEEE division and sqrtf, nudged one
+// ulp so the refinement is exercised.
+#pragma once
+
+#include <cstdint>
+#include <cstring>
+
+#ifndef __CUDACC__
+#define __host__
+#define __device__
+#define __forceinline__ inline
+#endif
+
+#include <cmath>
+
+namespace cbg {
+
+#define CB_HD __host__ __device__ __forceinline__
+
+struct ff {
+    float h, l;
+};
+
+// ---------------------------------------------------------------- bit casts
+CB_HD uint32_t ff_fbits(float f) {
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(f);
+#else
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+#endif
+}
+CB_HD float ff_bitsf(uint32_t u) {
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(u);
+#else
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+#endif
+}
+CB_HD uint64_t ff_dbits(double d) {
+#ifdef __CUDA_ARCH__
+    return (uint64_t)__double_as_longlong(d);
+#else
+    uint64_t u;
+    std::memcpy(&u, &d, 8);
+    return u;
+#endif
+}
+CB_HD double ff_bitsd(uint64_t u) {
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)u);
+#else
+    double d;
+    std::memcpy(&d, &u, 8);
+    return d;
+#endif
+}
+// The two 32-bit words of a double, and a double from them.
+CB_HD uint32_t ff_dhi(double d) {
+#ifdef __CUDA_ARCH__
+    return (uint32_t)__double2hiint(d);
+#else
+    return (uint32_t)(ff_dbits(d) >> 32);
+#endif
+}
+CB_HD uint32_t ff_dlo(double d) {
+#ifdef __CUDA_ARCH__
+    return (uint32_t)__double2loint(d);
+#else
+    return (uint32_t)ff_dbits(d);
+#endif
+}
+CB_HD double ff_mkd(uint32_t hi, uint32_t lo) {
+#ifdef __CUDA_ARCH__
+    return __hiloint2double((int)hi, (int)lo);
+#else
+    return ff_bitsd(((uint64_t)hi << 32) | lo);
+#endif
+}
+CB_HD float ff_fma(float a, float b, float c) {
+#ifdef __CUDA_ARCH__
+    return __fmaf_rn(a, b, c);
+#else
+    return std::fmaf(a, b, c);
+#endif
+}
+// Plain IEEE operations that the compiler must not contract into an FMA.
+CB_HD float ff_mulr(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+CB_HD float ff_addr(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+CB_HD float ff_subr(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fsub_rn(a, b);
+#else
+    return a - b;
+#endif
+}
+
+// FP32 estimates (~1 ulp) of 1/a and 1/sqrt(a), a > 0 normal.
+CB_HD float ff_rcp_est(float a) {
+#ifdef __CUDA_ARCH__
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a));
+    return r;
+#else
+    return std::nextafterf(1.0f / a, 1e30f);
+#endif
+}
+CB_HD float ff_rsqrt_est(float a) {
+#ifdef __CUDA_ARCH__
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a));
+    return r;
+#else
+    return std::nextafterf(1.0f / std::sqrt(a), 1e30f);
+#endif
+}
+
+// ------------------------------------------------- error-free transformations
+CB_HD ff two_sum(float a, float b) {  // a + b = s + e exactly
+    const float s = ff_addr(a, b);
+    const float bb = ff_subr(s, a);
+    const float e = ff_addr(ff_subr(a, ff_subr(s, bb)), ff_subr(b, bb));
+    return {s, e};
+}
+CB_HD ff fast_two_sum(float a, float b) {  // exact when |a| >= |b| (or a == 0)
+    const float s = ff_addr(a, b);
+    return {s, ff_subr(b, ff_subr(s, a))};
+}
+
+// ------------------------------------------------------ conversions
+// The top 24 bits of the significand (truncated) in h; the low 29 bits, rounded
+// to their top 23, in l; renormalised so that |l| <= 2^-24 |h|:
+// |x - (h + l)| <= 2^-47 |x|. The low part is built without an int -> float
+// conversion: the float 1.f 2^(E-23), whose fraction f is those 23 bits, less
+// 2^(E-23) (exact). |x| below 2^-103 keeps only the top bits (absolute error
+// < 2^-126); below 2^-126 gives 0. |x| must be below 2^128.
+CB_HD ff ff_of(double x) {
+    // 32-bit words only: 64-bit integer operations cost more issue slots
+    const uint32_t hi = ff_dhi(x), lo = ff_dlo(x);
+    const uint32_t sign = hi & 0x80000000u;
+    const int eb = (int)((hi >> 20) & 0x7ffu);  // biased double exponent
+    const int fe = eb - 896;                    // biased float exponent of h
+    if (fe <= 0) return {0.0f, 0.0f};
+    const uint32_t mant23 = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const float h = ff_bitsf(sign | ((uint32_t)fe << 23) | mant23);
+    const uint32_t rem = lo & 0x1fffffffu;  // the low 29 bits: rem 2^(E-52)
+    const int le = fe - 23;                 // biased float exponent of 2^(E-23)
+    float l = 0.0f;
+    if (le > 0) {
+        // (le << 23) + round(rem / 64): a carry out of the fraction gives 2^(E-22)
+        const uint32_t one = (uint32_t)le << 23;
+        l = ff_subr(ff_bitsf(one + ((rem + 32u) >> 6)), ff_bitsf(one));
+    }
+    return fast_two_sum(h, sign ? -l : l);
+}
+
+// Exact widening of a float (normal or zero) to double on the bit pattern.
+CB_HD double ff_f2d(float f) {
+    const uint32_t b = ff_fbits(f);
+    const uint32_t e = (b >> 23) & 0xffu;
+    if (e == 0) return 0.0;
+    return ff_mkd((b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3),
+                  (b & 7u) << 29);
+}
+
+// h + l rounded to double (error <= 1/2 ulp of the double) on the integer
+// pipe. Needs |l| <= 2^-24 |h| (a normalised pair: after fast_two_sum), h
+// normal or zero. With h's 24-bit significand the sum never reaches the next
+// binade; it can fall into the one below only when h is a power of two and l
+// has the opposite sign, where the double's ulp is half as large. l in units
+// of the double's ulp is below 2^31, so the low word takes it with one carry.
+CB_HD double ff_to_double(ff v) {
+    const uint32_t hb = ff_fbits(v.h), lb = ff_fbits(v.l);
+    const uint32_t he = (hb >> 23) & 0xffu, le = (lb >> 23) & 0xffu;
+    if (he == 0) return ff_f2d(v.l);
+    const uint32_t dhi = (hb & 0x80000000u) | ((he + 896u) << 20) | ((hb & 0x7fffffu) >> 3);
+    const uint32_t dlo = (hb & 7u) << 29;
+    if (le == 0) return ff_mkd(dhi, dlo);
+    const uint32_t lm = (lb & 0x7fffffu) | 0x800000u;  // 24-bit significand of l
+    const bool opp = ((hb ^ lb) & 0x80000000u) != 0;
+    const bool down = opp && (hb & 0x7fffffu) == 0;  // h = 2^E, result below 2^E
+    // l / ulp(h as double) = lm 2^(le - he + 29); one more bit when down
+    const int k = (int)le - (int)he + 29 + (down ? 1 : 0);
+    uint32_t delta;
+    if (k >= 0) {
+        delta = lm << k;  // k <= 6
+    } else if (k > -26) {
+        delta = (lm + (1u << (-k - 1))) >> (-k);
+    } else {
+        delta = 0u;
+    }
+    if (opp) {
+        const uint32_t lo2 = dlo - delta;
+        return ff_mkd(dhi - (dlo < delta ? 1u : 0u), lo2);
+    }
+    const uint32_t lo2 = dlo + delta;
+    return ff_mkd(dhi + (lo2 < dlo ? 1u : 0u), lo2);
+}
+
+// ------------------------------------------------------ arithmetic
+CB_HD ff ff_neg(ff a) { return {-a.h, -a.l}; }
+CB_HD ff ff_abs(ff a) { return a.h < 0.0f ? ff_neg(a) : a; }
+CB_HD ff ff_scale(ff a, float p2) { return {a.h * p2, a.l * p2}; }  // p2 a power of two
+
+// Sloppy double-word sum: relative error ~2^-46 without cancellation; with
+// cancellation the absolute error stays ~2^-47 (|a| + |b|).
+CB_HD ff ff_add(ff a, ff b) {
+    const ff s = two_sum(a.h, b.h);
+    const float e = ff_addr(s.l, ff_addr(a.l, b.l));
+    return fast_two_sum(s.h, e);
+}
+CB_HD ff ff_sub(ff a, ff b) { return ff_add(a, ff_neg(b)); }
+
+CB_HD ff ff_mul(ff a, ff b) {
+    const float p = ff_mulr(a.h, b.h);
+    float e = ff_fma(a.h, b.h, -p);
+    e = ff_fma(a.h, b.l, e);
+    e = ff_fma(a.l, b.h, e);
+    return fast_two_sum(p, e);
+}
+CB_HD ff ff_mul_f(ff a, float b) {
+    const float p = ff_mulr(a.h, b);
+    float e = ff_fma(a.h, b, -p);
+    e = ff_fma(a.l, b, e);
+    return fast_two_sum(p, e);
+}
+CB_HD ff ff_sqr(ff a) {
+    const float p = ff_mulr(a.h, a.h);
+    float e = ff_fma(a.h, a.h, -p);
+    e = ff_fma(ff_addr(a.h, a.h), a.l, e);
+    return fast_two_sum(p, e);
+}
+
+// 1/a, a > 0 with a.h a normal float.
+CB_HD ff ff_rcp(ff a) {
+    float y = ff_rcp_est(a.h);
+    y = ff_fma(y, ff_fma(-a.h, y, 1.0f), y);  // FP32 Newton step, |1 - a y| ~ 2^-24
+    const float th = ff_mulr(a.h, y);
+    float te = ff_fma(a.h, y, -th);
+    te = ff_fma(a.l, y, te);
+    const float e = ff_subr(ff_subr(1.0f, th), te);  // 1 - a y; 1 - th is exact
+    const float c = ff_fma(y, e, ff_mulr(ff_mulr(y, e), e));
+    return fast_two_sum(y, c);
+}
+
+// 1/sqrt(a), a > 0 with a.h a normal float.
+CB_HD ff ff_rsqrt(ff a) {
+    float y = ff_rsqrt_est(a.h);
+    const float hy = ff_mulr(0.5f, y);
+    y = ff_fma(hy, ff_fma(-ff_mulr(a.h, y), y, 1.0f), y);  // FP32 Newton step
+    const float sh = ff_mulr(y, y);
+    const float sl = ff_fma(y, y, -sh);  // y^2 = sh + sl exactly
+    const float th = ff_mulr(a.h, sh);
+    float te = ff_fma(a.h, sh, -th);
+    te = ff_fma(a.h, sl, te);
+    te = ff_fma(a.l, sh, te);
+    const float e = ff_subr(ff_subr(1.0f, th), te);  // 1 - a y^2
+    const float c = ff_fma(ff_mulr(0.5f, y), e, ff_mulr(ff_mulr(0.375f, e), ff_mulr(e, y)));
+    return fast_two_sum(y, c);
+}
+
+// sqrt(a) = a / sqrt(a) for a > 0, 0 otherwise.
+CB_HD ff ff_sqrt(ff a) {
+    if (!(a.h > 0.0f)) return {0.0f, 0.0f};
+    return ff_mul(a, ff_rsqrt(a));
+}
+
+// a - b evaluated to ~2^-46 (|a| + |b|), as one float: for sign tests.
+CB_HD float ff_diff_f(ff a, ff b) {
+    const ff s = two_sum(a.h, -b.h);
+    return ff_addr(s.h, ff_addr(s.l, ff_subr(a.l, b.l)));
+}
+
+#undef CB_HD
+
+}  // namespace cbg

@@ -23,6 +23,26 @@ __device__ __forceinline__ double4_32a ld4(const double *p, int i) {
     return reinterpret_cast<const double4_32a *>(p)[i];
 }
 
+// Float-float records of the float-float pair kernel (CB_PRECISION_FP64_FF):
+// (r, 1/r) and (r^2, 0) per bubble, written where the predicted radius is
+// known.
+struct FfRec {
+    ff r, inv, rsq;
+};
+__device__ __forceinline__ FfRec ld_rec(const float4 *R, int i) {
+    const float4 u = R[2 * (size_t)i], v = R[2 * (size_t)i + 1];
+    return {{u.x, u.y}, {u.z, u.w}, {v.x, v.y}};
+}
+__device__ __forceinline__ void st_rec(float4 *R, int i, double r, double inv, double rsq) {
+    const ff a = ff_of(r), b = ff_of(inv), c = ff_of(rsq);
+    R[2 * (size_t)i] = make_float4(a.h, a.l, b.h, b.l);
+    R[2 * (size_t)i + 1] = make_float4(c.h, c.l, 0.f, 0.f);
+}
+__device__ __forceinline__ bool ff_less(ff a, ff b) {  // normalised pairs
+    return a.h < b.h || (a.h == b.h && a.l < b.l);
+}
+__device__ __forceinline__ void add_d(double *p, ff v) { atomicAdd(p, ff_to_double(v)); }
+
 // ---------------------------------------------------------------- predict
 template <int DIM>
 __device__ __forceinline__ void k_predict_body(const Bufs &b, const int vb, const int vg) {
@@ -45,13 +65,15 @@ __device__ __forceinline__ void k_predict_body(const Bufs &b, const int vb, cons
         double rp = R[i];
         if (gas) rp = fma(h, fma(3.0, V3[i], -O3[i]), rp);
         const double inv = rcp_hn(rp);
+        const double rsq = rp * rp;
+        if (b.ffr) st_rec(b.ffr, i, rp, inv, rsq);
         double4_32a p;
         if (DIM == 3) {
             p.x = xp;
             p.y = yp;
             p.z = fma(h, fma(3.0, V2[i], -O2[i]), Z[i]);
             p.w = rp;
-            reinterpret_cast<double2 *>(b.invr)[i] = make_double2(inv, rp * rp);
+            reinterpret_cast<double2 *>(b.invr)[i] = make_double2(inv, rsq);
         } else {
             p.x = xp;
             p.y = yp;
@@ -208,6 +230,197 @@ __device__ __forceinline__ void k_pairs_body(const Bufs &b, const int vb, const 
     }
 }
 CB_KERNEL_PAIR((template <int DIM, bool GAS, bool FLOW>), k_pairs, (<DIM, GAS, FLOW>), __launch_bounds__(kBlock))
+
+
+// ------------------------------------------------------ pairs, float-float
+// CB_PRECISION_FP64_FF: the pair kernel of the FP64 form with its arithmetic
+// in float-float. Overlap velocities, pairwise gas flux and overlap areas
+// (pairwiseInteraction, src/kernels.cu:172-337). GB300 issues FP64 at 1/64 of
+// the FP32 rate, so apart from the three FP64 position differences
+// (wrappedDifference, src/kernels.cu:1094-1114) the pair arithmetic runs in
+// float-float (ff.cuh, ~2^-46 relative) on the FP32 and integer pipes, from
+// per-bubble float-float records (r, 1/r, r^2) written by k_predict. The
+// overlap test and the inside tests of the gas exchange are decided in
+// float-float unless the difference is within 2^-38 of its operands; then the
+// FP64 comparisons of the reference decide, so the classification of every
+// pair is the FP64 one.
+//
+// Each thread takes a run of kRun consecutive pairs (rows are grouped by i):
+// the i-side sums stay in float-float registers and go out once per row; the
+// j-side contributions go out per pair. Both are rounded to double on the
+// integer pipe and added to the FP64 accumulator rows with FP64 atomics.
+constexpr int kRun = 4;
+constexpr float kAmb = 0x1p-38f;
+
+
+template <int DIM, bool GAS, bool FLOW>
+__device__ __forceinline__ void k_pairs_ff_body(const Bufs &b, const int vb, const int vg) {
+    __shared__ double smem[32];
+    const Ctrl *c = b.ctrl;
+    const DevConst &k = *b.k;
+    const int np = c->np;
+    const int *PI = b.ps[c->prole[PI0]];
+    const int *PJ = b.ps[c->prole[PJ0]];
+    const double *V0 = drow(b, c, RV0), *V1 = drow(b, c, RV1), *V2 = drow(b, c, RV2);
+    const float4 *REC = b.ffr;
+    const ff f0 = {k.f0_f, k.f0_l};
+    const ff pi = {(float)kPi, (float)(kPi - (double)(float)kPi)};
+    const bool px = !k.wall[0], py = !k.wall[1], pz = DIM == 3 && !k.wall[2];
+    const double hx = k.half_iv[0], hy = k.half_iv[1], hz = k.half_iv[2];
+    const double Lx = k.iv[0], Ly = k.iv[1], Lz = k.iv[2];
+    ff sAo = {0.f, 0.f}, sAor = {0.f, 0.f};
+    const int nrun = (np + kRun - 1) / kRun;
+    for (int g = vb * blockDim.x + threadIdx.x; g < nrun; g += vg * blockDim.x) {
+        const int p0 = g * kRun;
+        int cur = -1;
+        double4_32a a;
+        FfRec ra;
+        ff ax = {0.f, 0.f}, ay = ax, az = ax, ag = ax, ao = ax;
+        bool hit = false;
+        double vxi = 0.0, vyi = 0.0, vzi = 0.0;
+        auto flush = [&](int i) {
+            double *ai = b.acc + (size_t)i * kAcc;
+            add_d(ai + 0, ax);
+            add_d(ai + 1, ay);
+            if (DIM == 3) add_d(ai + 2, az);
+            if (GAS) {
+                add_d(ai + 3, ag);
+                add_d(ai + 4, ao);
+            }
+        };
+#pragma unroll 1  // one pair body: the unrolled run overflows the instruction cache
+        for (int t = 0; t < kRun; t++) {
+            if (p0 + t >= np) break;
+            const int i = PI[p0 + t], j = PJ[p0 + t];
+            if (i != cur) {
+                if (hit) flush(cur);
+                cur = i;
+                a = ld4(b.pred, i);
+                ra = ld_rec(REC, i);
+                ax = ay = az = ag = ao = ff{0.f, 0.f};
+                hit = false;
+                if (FLOW) {
+                    vxi = V0[i];
+                    vyi = V1[i];
+                    vzi = DIM == 3 ? V2[i] : 0.0;
+                }
+            }
+            double *aj = b.acc + (size_t)j * kAcc;
+            if (FLOW) {  // src/kernels.cu:191-207 (added for every pair)
+                atomicAdd(aj + 5, vxi);
+                atomicAdd(aj + 6, vyi);
+                if (DIM == 3) atomicAdd(aj + 7, vzi);
+            }
+            const double4_32a q = ld4(b.pred, j);
+            const FfRec rb = ld_rec(REC, j);
+            // wrappedDifference, src/kernels.cu:1094-1114 (FP64)
+            double dx = a.x - q.x, dy = a.y - q.y, dz = 0.0;
+            if (px) dx = min_image(dx, hx, Lx);
+            if (py) dy = min_image(dy, hy, Ly);
+            if (DIM == 3) {
+                dz = a.z - q.z;
+                if (pz) dz = min_image(dz, hz, Lz);
+            }
+            const ff X = ff_of(dx), Y = ff_of(dy), Z = ff_of(dz);
+            ff m = ff_add(ff_sqr(X), ff_sqr(Y));
+            if (DIM == 3) m = ff_add(m, ff_sqr(Z));
+            const ff R = ff_add(ra.r, rb.r);
+            const ff RR = ff_sqr(R);
+            const float dov = ff_diff_f(RR, m);
+            bool over = dov >= 0.f;
+            bool amb = fabsf(dov) <= kAmb * RR.h;
+            bool inside = false;
+            if (GAS) {
+                const float d1 = ff_diff_f(m, ra.rsq), d2 = ff_diff_f(m, rb.rsq);
+                inside = d1 < 0.f || d2 < 0.f;
+                amb |= fabsf(d1) <= kAmb * m.h || fabsf(d2) <= kAmb * m.h;
+            }
+            if (amb) {  // within 2^-38: the reference's FP64 tests decide
+                double m64 = dx * dx;
+                m64 = fma(dy, dy, m64);
+                if (DIM == 3) m64 = fma(dz, dz, m64);
+                const double r1 = DIM == 3 ? a.w : a.z, r2 = DIM == 3 ? q.w : q.z;
+                const double radii = r1 + r2;
+                over = nonneg_bits(fma(radii, radii, -m64));
+                if (GAS) {
+                    double r1sq, r2sq;
+                    if (DIM == 3) {
+                        r1sq = b.invr[2 * (size_t)i + 1];
+                        r2sq = b.invr[2 * (size_t)j + 1];
+                    } else {
+                        r1sq = r1 * r1;
+                        r2sq = r2 * r2;
+                    }
+                    inside = less_nonneg(m64, r1sq) || less_nonneg(m64, r2sq);
+                }
+            }
+            if (!over) continue;
+            // velocity f0 d (1/|d| - 1/(r1 + r2)), src/kernels.cu:218-233
+            const ff rs = ff_rsqrt(m);
+            const ff s = ff_mul(f0, ff_sub(rs, ff_rcp(R)));
+            const ff fx = ff_mul(X, s), fy = ff_mul(Y, s);
+            ax = ff_add(ax, fx);
+            ay = ff_add(ay, fy);
+            add_d(aj + 0, ff_neg(fx));
+            add_d(aj + 1, ff_neg(fy));
+            if (DIM == 3) {
+                const ff fz = ff_mul(Z, s);
+                az = ff_add(az, fz);
+                add_d(aj + 2, ff_neg(fz));
+            }
+            hit = true;
+            if (GAS) {  // pairwise gas exchange, src/kernels.cu:236-280
+                // chord: r2^2 - t^2 / m with t = (r2^2 - r1^2 + m) / 2, as
+                // r2^2 - w^2 / 4 with w = (r2^2 - r1^2 + m) / |d|
+                ff oa;
+                if (inside) {
+                    if (DIM == 3)
+                        oa = ff_mul(ff_less(ra.rsq, rb.rsq) ? ra.rsq : rb.rsq, pi);
+                    else
+                        oa = ff_scale(ff_less(ra.r, rb.r) ? ra.r : rb.r, 2.f);
+                } else {
+                    const ff w = ff_mul(ff_add(ff_sub(rb.rsq, ra.rsq), m), rs);
+                    const ff v = ff_abs(ff_sub(rb.rsq, ff_scale(ff_sqr(w), 0.25f)));
+                    oa = DIM == 3 ? ff_mul(v, pi) : ff_scale(ff_sqrt(v), 2.f);
+                }
+                const ff gf = ff_mul(oa, ff_sub(rb.inv, ra.inv));
+                ag = ff_add(ag, gf);
+                ao = ff_add(ao, oa);
+                add_d(aj + 3, ff_neg(gf));
+                add_d(aj + 4, oa);
+                sAo = ff_add(sAo, oa);
+                sAor = ff_add(sAor, ff_mul(oa, ff_add(ra.inv, rb.inv)));
+            }
+            if (FLOW) {  // src/kernels.cu:298-307 (overlapping pairs only)
+                double *ai = b.acc + (size_t)i * kAcc;
+                atomicAdd(ai + 5, V0[j]);
+                atomicAdd(ai + 6, V1[j]);
+                if (DIM == 3) atomicAdd(ai + 7, V2[j]);
+            }
+        }
+        if (hit) flush(cur);
+    }
+    const double tAo = block_reduce(ff_to_double(sAo), OpSum(), smem);
+    const double tAor = block_reduce(ff_to_double(sAor), OpSum(), smem);
+    if (threadIdx.x == 0) {
+        b.part[2 * vg + vb] = tAo;
+        b.part[3 * vg + vb] = tAor;
+    }
+    if (last_block(&b.ctrl->done[DC_PAIRS], vg)) {
+        const double fAo = fold_partials(b.part + 2 * vg, vg, false, smem);
+        const double fAor = fold_partials(b.part + 3 * vg, vg, false, smem);
+        if (threadIdx.x == 0) {
+            Ctrl *cc = b.ctrl;
+            cc->sumAo = 2.0 * fAo;  // each pair adds 2 A_overlap, :267
+            cc->sumAor = fAor;
+            // mean-field factors for every bubble, src/kernels.cu:399-404
+            cc->mfa = (cc->sumAr - cc->sumAor) / (cc->sumA - cc->sumAo);
+            cc->mfb = k.kappa * k.ain * (double)cc->n / cc->sumA;
+            cc->done[DC_PAIRS] = 0;
+        }
+    }
+}
+CB_KERNEL_PAIR((template <int DIM, bool GAS, bool FLOW>), k_pairs_ff, (<DIM, GAS, FLOW>), __launch_bounds__(kBlock, 3))
 
 
 // ---------------------------------------------------------------- correct
@@ -438,13 +651,15 @@ __global__ void __launch_bounds__(kBlock) k_boot(Bufs b, int phase) {
             const double r = R[i];
             p.x = X[i];
             p.y = Y[i];
+            const double inv = 1.0 / r, rsq = r * r;
+            if (b.ffr) st_rec(b.ffr, i, r, inv, rsq);
             if (DIM == 3) {
                 p.z = Z[i];
                 p.w = r;
-                reinterpret_cast<double2 *>(b.invr)[i] = make_double2(1.0 / r, r * r);
+                reinterpret_cast<double2 *>(b.invr)[i] = make_double2(inv, rsq);
             } else {
                 p.z = r;
-                p.w = 1.0 / r;
+                p.w = inv;
             }
             P[i] = p;
             O0[i] = O1[i] = O2[i] = O3[i] = 0.0;
@@ -544,9 +759,15 @@ void launch_predict(const Launch &l, const Bufs &b, int dim) {
 }
 
 // mode bits: 1 = gas exchange, 2 = flow. mode 0 is the bootstrap form.
-void launch_pairs(const Launch &l, const Bufs &b, int dim, int mode) {
+void launch_pairs(const Launch &l, const Bufs &b, int dim, int mode, bool ff) {
     const bool gas = mode & 1, flow = mode & 2;
-#define CB_PAIRS(D, G, F) CB_LAUNCH(l, k_pairs, (<D, G, F>), wave_grid(k_pairs<D, G, F>, l), b)
+#define CB_PAIRS(D, G, F)                                                                     \
+    do {                                                                                      \
+        if (ff)                                                                               \
+            CB_LAUNCH(l, k_pairs_ff, (<D, G, F>), wave_grid(k_pairs_ff<D, G, F>, l), b);      \
+        else                                                                                  \
+            CB_LAUNCH(l, k_pairs, (<D, G, F>), wave_grid(k_pairs<D, G, F>, l), b);            \
+    } while (0)
     if (dim == 3) {
         if (gas && flow) CB_PAIRS(3, true, true);
         else if (gas) CB_PAIRS(3, true, false);

@@ -45,6 +45,10 @@ extern "C" {
 #define CB_PRECISION_FP64 0  /* plain FP64 form (reference arithmetic)        */
 #define CB_PRECISION_MIXED 1 /* FP32 pair geometry on exact 64-bit fixed-point
                                 differences, FP64 positions/volume/error     */
+#define CB_PRECISION_FP64_FF 2 /* the FP64 form with its pair terms (distance,
+                                velocities, gas flux, overlap areas) in
+                                float-float (two FP32, ~2^-46 relative) on the
+                                FP32 pipe; FP64 state, update and sums       */
 
 /* ------------------------------------------------------------ constants */
 /* Mirrors `Constants` (src/data_definitions.h:183-225) plus the host-side

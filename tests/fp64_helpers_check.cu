@@ -29,3 +29,28 @@ extern "C" int fp64_check(const double *host_in, int n, double *host_out) {
     cudaFree(dout);
     return e == cudaSuccess ? 0 : 2;
 }
+
+// The float-float helpers of the FP64 pair kernel (ff.cuh) on the device,
+// where the FP32 estimates come from the hardware approximations: split and
+// back, reciprocal, rsqrt and sqrt, each rounded back to double.
+__global__ void k_ff_check(const double *in, int n, double *out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const cbg::ff a = cbg::ff_of(in[i]);
+        out[4 * i + 0] = cbg::ff_to_double(cbg::fast_two_sum(a.h, a.l));
+        out[4 * i + 1] = cbg::ff_to_double(cbg::ff_rcp(a));
+        out[4 * i + 2] = cbg::ff_to_double(cbg::ff_rsqrt(a));
+        out[4 * i + 3] = cbg::ff_to_double(cbg::ff_sqrt(a));
+    }
+}
+
+extern "C" int ff_check(const double *host_in, int n, double *host_out) {
+    double *din = nullptr, *dout = nullptr;
+    if (cudaMalloc(&din, n * sizeof(double)) != cudaSuccess) return 1;
+    if (cudaMalloc(&dout, 4 * n * sizeof(double)) != cudaSuccess) return 1;
+    cudaMemcpy(din, host_in, n * sizeof(double), cudaMemcpyHostToDevice);
+    k_ff_check<<<256, 256>>>(din, n, dout);
+    cudaError_t e = cudaMemcpy(host_out, dout, 4 * n * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaFree(din);
+    cudaFree(dout);
+    return e == cudaSuccess ? 0 : 2;
+}

@@ -78,6 +78,11 @@ def test_batch_fp64_matches_single():
     compare_with_single(small_sweep(count=4, precision=0, graph=1), 0, 1, 25, 1e-12)
 
 
+def test_batch_fp64_ff_matches_single():
+    """The FP64 form with float-float pair terms, batched and alone."""
+    compare_with_single(small_sweep(count=4, precision=2, graph=1), 2, 1, 25, 1e-12)
+
+
 def test_batch_fp64_against_oracle(oracle_mod):
     items = small_sweep(count=3, precision=0, graph=1)
     batch = cb.GpuFoamBatch([c for c, _ in items])

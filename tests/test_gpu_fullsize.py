@@ -10,7 +10,10 @@ properties that do not depend on an oracle run of that size:
     of their magnitudes, 1e-12 in FP64);
   * a second search of an unchanged state reproduces the list (idempotence);
   * the mixed form matches the FP64 form within its stated bars at full
-    size (one attempt 1e-6 per row, 20 steps: same counts, volume 1e-10).
+    size (one attempt 1e-6 per row, 20 steps: same counts, volume 1e-10);
+  * the FP64 form with float-float pair terms matches the plain FP64 form
+    within the FP64 bar (one attempt 1e-12 per row, 20 steps: same counts,
+    volume 1e-12).
 """
 import numpy as np
 import pytest
@@ -118,5 +121,38 @@ def test_mixed_matches_fp64_at_full_size(c2):
     assert ra["count"] == rb["count"]
     assert b.total_volume() == pytest.approx(a.total_volume(), rel=1e-10)
     assert a.total_volume() == pytest.approx(v0, rel=1e-9)
+    a.close()
+    b.close()
+
+
+def test_ff_form_matches_fp64_at_full_size(c2):
+    cfg, st = c2
+    a = cb.GpuFoam(cfg)
+    a.load_state(st)
+    workloads.prepare(a)
+    a.integrate(3)
+    s0 = a.get_state()
+    i, j = a.pairs()
+    cfg_f, _ = workloads.config_c2(n=N, precision=2)
+    b = cb.GpuFoam(cfg_f)
+    b.load_state(s0)
+    b.set_pairs(i, j)
+    b.set_time(a.report()["time_step"])
+    aa, ab = a.attempt(), b.attempt()
+    for k, base in (("xp", "x"), ("yp", "y"), ("zp", "z")):
+        d = ab[k] - aa[k]
+        m = aa[k] - s0[base]
+        assert np.max(np.abs(d)) <= 1e-12 * np.max(np.abs(m)) + 4 * np.spacing(
+            np.max(np.abs(aa[k]))), k
+    for k in ("dxdtp", "dydtp", "dzdtp", "drdtp", "overlap"):
+        assert np.max(np.abs(ab[k] - aa[k])) <= 1e-12 * np.max(np.abs(aa[k])), k
+    for k in ("total_overlap_area", "total_overlap_area_per_radius"):
+        assert ab[k] == pytest.approx(aa[k], rel=1e-12), k
+    qa, qb = a.report(), b.report()
+    ra, rb = a.integrate(20), b.integrate(20)
+    for k in ("steps", "attempts", "searches", "deleted"):
+        assert ra[k] - qa[k] == rb[k] - qb[k], k
+    assert ra["count"] == rb["count"]
+    assert b.total_volume() == pytest.approx(a.total_volume(), rel=1e-12)
     a.close()
     b.close()

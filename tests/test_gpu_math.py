@@ -47,3 +47,20 @@ def test_min_image_matches_reference_formula(checker):
     out = np.zeros((len(x), 8))
     assert checker.fp64_check(x.ctypes.data, len(x), out.ctypes.data) == 0
     assert np.array_equal(out[:, 6], out[:, 7])
+
+
+def test_float_float_helpers_on_device(checker):
+    """The FP64 pair kernel's float-float reciprocal, rsqrt and sqrt with the
+    hardware FP32 estimates: within 2^-45 of the exact values (long double),
+    and the split of a double keeps 2^-47 of it."""
+    checker.ff_check.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    rng = np.random.default_rng(1)
+    x = np.concatenate([np.logspace(-20, 20, 100001), rng.uniform(1e-3, 50.0, 100000)])
+    out = np.zeros((len(x), 4))
+    assert checker.ff_check(x.ctypes.data, len(x), out.ctypes.data) == 0
+    L = x.astype(np.longdouble)
+    rel = lambda a, b: np.max(np.abs(a.astype(np.longdouble) - b) / np.abs(b))  # noqa: E731
+    assert rel(out[:, 0], L) <= 2.0 ** -47
+    assert rel(out[:, 1], 1 / L) <= 2.0 ** -45
+    assert rel(out[:, 2], 1 / np.sqrt(L)) <= 2.0 ** -45
+    assert rel(out[:, 3], np.sqrt(L)) <= 2.0 ** -45
