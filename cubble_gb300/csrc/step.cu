@@ -41,7 +41,9 @@ __device__ __forceinline__ void st_rec(float4 *R, int i, double r, double inv, d
 __device__ __forceinline__ bool ff_less(ff a, ff b) {  // normalised pairs
     return a.h < b.h || (a.h == b.h && a.l < b.l);
 }
-__device__ __forceinline__ void add_d(double *p, ff v) { atomicAdd(p, ff_to_double(v)); }
+__device__ __forceinline__ void add_d(double *p, ff v) {
+    asm volatile("red.global.add.f64 [%0], %1;" ::"l"(p), "d"(ff_to_double(v)));
+}
 
 // ---------------------------------------------------------------- predict
 template <int DIM>
@@ -107,14 +109,40 @@ CB_KERNEL_PAIR((template <int DIM>), k_predict, (<DIM>), __launch_bounds__(kBloc
 
 
 // ------------------------------------------------------------------ pairs
-// One lane per pair; contributions to both members go through FP64 atomics
-// into the per-bubble accumulator rows. FP64-issue bound on GB300, so:
-// minimum image by bit compare, 1/sqrt(m) and 1/(r1 + r2) by rsqrt_hn /
-// rcp_hn, the division by m of the overlap formula as a product with
-// (1/sqrt(m))^2.
+// Overlap velocities, pairwise gas flux and overlap areas in FP64
+// (pairwiseInteraction, src/kernels.cu:172-337). FP64-issue bound on GB300
+// (2 FP64 thread-instructions per SM and cycle), so:
+//   * each warp takes 32 consecutive pairs, computes their FP64 geometry and
+//     overlap test (8 FP64 instructions a pair), and queues the overlapping
+//     ones (about 70 % of the listed pairs) in shared memory; the force and
+//     gas-exchange arithmetic (~23 FP64 instructions) then runs on full warps
+//     of overlapping pairs, not on warps with idle lanes;
+//   * minimum image by bit compare, 1/sqrt(m) and 1/(r1 + r2) by rsqrt_hn /
+//     rcp_hn, the division by m of the overlap formula as a product with
+//     (1/sqrt(m))^2, -w/4 on the exponent field;
+//   * contributions to both members go through FP64 reductions into the
+//     per-bubble accumulator rows.
+__device__ __forceinline__ void red_add(double *p, double v) {
+    asm volatile("red.global.add.f64 [%0], %1;" ::"l"(p), "d"(v));
+}
+// -w/4, exact: the exponent field lowered by 2 and the sign flipped when the
+// exponent allows it (|w| > 2^-1020), else the FP64 product.
+__device__ __forceinline__ double neg_quarter(double w) {
+    const int hi = __double2hiint(w);
+    if ((hi & 0x7ff00000) > 0x00200000)
+        return __hiloint2double((hi - 0x00200000) ^ (int)0x80000000, __double2loint(w));
+    return -0.25 * w;
+}
+
+constexpr int kQueue = 64;  // per-warp queue of overlapping pairs
+
 template <int DIM, bool GAS, bool FLOW>
 __device__ __forceinline__ void k_pairs_body(const Bufs &b, const int vb, const int vg) {
+    constexpr int kW = kBlock / 32;
     __shared__ double smem[32];
+    // queue slots: dx, dy, dz (2D: r1), m, r1 + r2, (2D: r2)
+    __shared__ double qd[kW][DIM == 3 ? 5 : 6][kQueue];
+    __shared__ int qij[kW][2][kQueue];
     const Ctrl *c = b.ctrl;
     const DevConst &k = *b.k;
     const int np = c->np;
@@ -125,90 +153,148 @@ __device__ __forceinline__ void k_pairs_body(const Bufs &b, const int vb, const 
     const bool px = !k.wall[0], py = !k.wall[1], pz = DIM == 3 && !k.wall[2];
     const double hx = k.half_iv[0], hy = k.half_iv[1], hz = k.half_iv[2];
     const double Lx = k.iv[0], Ly = k.iv[1], Lz = k.iv[2];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned below = (1u << lane) - 1u;
+    double(*Q)[kQueue] = qd[w];
+    int *QI = qij[w][0], *QJ = qij[w][1];
     double sAo = 0.0, sAor = 0.0;
-    for (int p = vb * blockDim.x + threadIdx.x; p < np; p += vg * blockDim.x) {
-        const int i = PI[p], j = PJ[p];
+
+    // the force and gas-exchange terms of queued (overlapping) pair e
+    auto process = [&](int e) {
+        const int i = QI[e], j = QJ[e];
+        const double dx = Q[0][e], dy = Q[1][e], m = Q[3][e], radii = Q[4][e];
+        const double dz = DIM == 3 ? Q[2][e] : 0.0;
         double *ai = b.acc + (size_t)i * kAcc;
         double *aj = b.acc + (size_t)j * kAcc;
-        if (FLOW) {  // src/kernels.cu:191-207 (added for every pair)
-            atomicAdd(aj + 5, V0[i]);
-            atomicAdd(aj + 6, V1[i]);
-            if (DIM == 3) atomicAdd(aj + 7, V2[i]);
-        }
-        const double4_32a a = ld4(b.pred, i), q = ld4(b.pred, j);
-        const double r1 = DIM == 3 ? a.w : a.z, r2 = DIM == 3 ? q.w : q.z;
-        // wrappedDifference, src/kernels.cu:1094-1114
-        double dx = a.x - q.x, dy = a.y - q.y, dz = 0.0;
-        if (px) dx = min_image(dx, hx, Lx);
-        if (py) dy = min_image(dy, hy, Ly);
+        // velocity f0 d (1/|d| - 1/(r1 + r2)), src/kernels.cu:218-233
+        const double rs = rsqrt_hn(m);
+        const double s = f0 * (rs - rcp_hn(radii));
+        const double fx = dx * s, fy = dy * s;
+        red_add(ai + 0, fx);
+        red_add(aj + 0, neg_bits(fx));
+        red_add(ai + 1, fy);
+        red_add(aj + 1, neg_bits(fy));
         if (DIM == 3) {
-            dz = a.z - q.z;
-            if (pz) dz = min_image(dz, hz, Lz);
+            const double fz = dz * s;
+            red_add(ai + 2, fz);
+            red_add(aj + 2, neg_bits(fz));
         }
-        double m = dx * dx;
-        m = fma(dy, dy, m);
-        if (DIM == 3) m = fma(dz, dz, m);
-        const double radii = r1 + r2;
-        // overlap test radii^2 >= m on the sign of the exact difference
-        if (nonneg_bits(fma(radii, radii, -m))) {
-            // velocity f0 d (1/|d| - 1/(r1 + r2)), src/kernels.cu:218-233
-            const double rs = rsqrt_hn(m);
-            const double s = f0 * (rs - rcp_hn(radii));
-            const double fx = dx * s, fy = dy * s;
-            atomicAdd(ai + 0, fx);
-            atomicAdd(aj + 0, neg_bits(fx));
-            atomicAdd(ai + 1, fy);
-            atomicAdd(aj + 1, neg_bits(fy));
+        if (GAS) {  // pairwise gas exchange, src/kernels.cu:236-280
+            double r1sq, r2sq, inv1, inv2, r1 = 0.0, r2 = 0.0;
+            if (DIM == 3) {  // (1/r, r^2) records written by k_predict
+                const double2 e1 = reinterpret_cast<const double2 *>(b.invr)[i];
+                const double2 e2 = reinterpret_cast<const double2 *>(b.invr)[j];
+                inv1 = e1.x;
+                r1sq = e1.y;
+                inv2 = e2.x;
+                r2sq = e2.y;
+            } else {
+                r1 = Q[2][e];
+                r2 = Q[5][e];
+                r1sq = r1 * r1;
+                r2sq = r2 * r2;
+                inv1 = b.pred[4 * (size_t)i + 3];
+                inv2 = b.pred[4 * (size_t)j + 3];
+            }
+            const bool inside = less_nonneg(m, r1sq) || less_nonneg(m, r2sq);
+            // chord: r2^2 - t^2 / m with t = (r2^2 - r1^2 + m) / 2, as
+            // r2^2 - w^2 / 4 with w = (r2^2 - r1^2 + m) / |d|
+            double oa;
             if (DIM == 3) {
-                const double fz = dz * s;
-                atomicAdd(ai + 2, fz);
-                atomicAdd(aj + 2, neg_bits(fz));
-            }
-            if (GAS) {  // pairwise gas exchange, src/kernels.cu:236-280
-                // 3D: (1/r, r^2) records written by k_predict
-                double2 e1 = make_double2(0.0, 0.0), e2 = e1;
-                if (DIM == 3) {
-                    e1 = reinterpret_cast<const double2 *>(b.invr)[i];
-                    e2 = reinterpret_cast<const double2 *>(b.invr)[j];
-                }
-                const double r1sq = DIM == 3 ? e1.y : r1 * r1, r2sq = DIM == 3 ? e2.y : r2 * r2;
-                const bool inside = less_nonneg(m, r1sq) || less_nonneg(m, r2sq);
-                // chord: r2^2 - t^2 / m with t = (r2^2 - r1^2 + m) / 2, as
-                // r2^2 - w^2 / 4 with w = (r2^2 - r1^2 + m) / |d|
-                double oa;
-                if (DIM == 3) {
-                    if (inside) {
-                        oa = min_nonneg(r1sq, r2sq);
-                    } else {
-                        const double w = (r2sq - r1sq + m) * rs;
-                        oa = abs_bits(fma(-0.25 * w, w, r2sq));
-                    }
-                    oa *= kPi;
+                if (inside) {
+                    oa = min_nonneg(r1sq, r2sq);
                 } else {
-                    if (inside) {
-                        oa = 2.0 * min_nonneg(r1, r2);
-                    } else {
-                        const double w = (r2sq - r1sq + m) * rs;
-                        oa = 2.0 * sqrt_hn(abs_bits(fma(-0.25 * w, w, r2sq)));
-                    }
+                    const double wv = (r2sq - r1sq + m) * rs;
+                    oa = abs_bits(fma(neg_quarter(wv), wv, r2sq));
                 }
-                const double inv1 = DIM == 3 ? e1.x : a.w;
-                const double inv2 = DIM == 3 ? e2.x : q.w;
-                const double g = oa * (inv2 - inv1);
-                atomicAdd(ai + 3, g);
-                atomicAdd(aj + 3, neg_bits(g));
-                atomicAdd(ai + 4, oa);
-                atomicAdd(aj + 4, oa);
-                sAo += oa;
-                sAor = fma(oa, inv1 + inv2, sAor);
+                oa *= kPi;
+            } else {
+                if (inside) {
+                    oa = 2.0 * min_nonneg(r1, r2);
+                } else {
+                    const double wv = (r2sq - r1sq + m) * rs;
+                    oa = 2.0 * sqrt_hn(abs_bits(fma(neg_quarter(wv), wv, r2sq)));
+                }
             }
-            if (FLOW) {  // src/kernels.cu:298-307 (overlapping pairs only)
-                atomicAdd(ai + 5, V0[j]);
-                atomicAdd(ai + 6, V1[j]);
-                if (DIM == 3) atomicAdd(ai + 7, V2[j]);
+            const double g = oa * (inv2 - inv1);
+            red_add(ai + 3, g);
+            red_add(aj + 3, neg_bits(g));
+            red_add(ai + 4, oa);
+            red_add(aj + 4, oa);
+            sAo += oa;
+            sAor = fma(oa, inv1 + inv2, sAor);
+        }
+        if (FLOW) {  // src/kernels.cu:298-307 (overlapping pairs only)
+            red_add(ai + 5, V0[j]);
+            red_add(ai + 6, V1[j]);
+            if (DIM == 3) red_add(ai + 7, V2[j]);
+        }
+    };
+
+    int cnt = 0;  // queued pairs of this warp (uniform over its lanes)
+    const int nch = (np + 31) >> 5;
+    for (int ch = vb * kW + w; ch < nch; ch += vg * kW) {
+        const int p = (ch << 5) + lane;
+        bool over = false;
+        int i = 0, j = 0;
+        double dx = 0.0, dy = 0.0, dz = 0.0, m = 0.0, radii = 0.0, r1 = 0.0, r2 = 0.0;
+        if (p < np) {
+            i = PI[p];
+            j = PJ[p];
+            if (FLOW) {  // src/kernels.cu:191-207 (added for every pair)
+                double *aj = b.acc + (size_t)j * kAcc;
+                red_add(aj + 5, V0[i]);
+                red_add(aj + 6, V1[i]);
+                if (DIM == 3) red_add(aj + 7, V2[i]);
             }
+            const double4_32a a = ld4(b.pred, i), q = ld4(b.pred, j);
+            r1 = DIM == 3 ? a.w : a.z;
+            r2 = DIM == 3 ? q.w : q.z;
+            // wrappedDifference, src/kernels.cu:1094-1114
+            dx = a.x - q.x;
+            dy = a.y - q.y;
+            if (px) dx = min_image(dx, hx, Lx);
+            if (py) dy = min_image(dy, hy, Ly);
+            if (DIM == 3) {
+                dz = a.z - q.z;
+                if (pz) dz = min_image(dz, hz, Lz);
+            }
+            m = dx * dx;
+            m = fma(dy, dy, m);
+            if (DIM == 3) m = fma(dz, dz, m);
+            radii = r1 + r2;
+            // overlap test radii^2 >= m on the sign of the exact difference
+            over = nonneg_bits(fma(radii, radii, -m));
+        }
+        const unsigned mask = __ballot_sync(0xffffffffu, over);
+        if (over) {
+            const int e = cnt + __popc(mask & below);
+            QI[e] = i;
+            QJ[e] = j;
+            Q[0][e] = dx;
+            Q[1][e] = dy;
+            Q[2][e] = DIM == 3 ? dz : r1;
+            Q[3][e] = m;
+            Q[4][e] = radii;
+            if (DIM == 2) Q[5][e] = r2;
+        }
+        cnt += __popc(mask);
+        __syncwarp();
+        if (cnt >= 32) {  // a full warp of overlapping pairs
+            process(lane);
+            __syncwarp();
+            cnt -= 32;
+            if (lane < cnt) {
+                QI[lane] = QI[32 + lane];
+                QJ[lane] = QJ[32 + lane];
+#pragma unroll
+                for (int t = 0; t < (DIM == 3 ? 5 : 6); t++) Q[t][lane] = Q[t][32 + lane];
+            }
+            __syncwarp();
         }
     }
+    if (lane < cnt) process(lane);
+
     const double tAo = block_reduce(sAo, OpSum(), smem);
     const double tAor = block_reduce(sAor, OpSum(), smem);
     if (threadIdx.x == 0) {
