@@ -357,6 +357,17 @@ __device__ __forceinline__ double rsqrt_hn(double a) {
     const double e = fma(-t, y, 1.0);
     return fma(y * e, fma(e, 0.375, 0.5), y);
 }
+// 1/sqrt(a) and 1/a to ~1 ulp with 2 and 1 FP64 instructions (ff.cuh);
+// rsqrt_hn / rcp_hn outside the float-float range.
+static __device__ __noinline__ double rsqrt_slow(double a) { return rsqrt_hn(a); }
+static __device__ __noinline__ double rcp_slow(double a) { return rcp_hn(a); }
+__device__ __forceinline__ double rsqrt_d(double a) {
+    return ff_in_range(a) ? rsqrt_d_core(a) : rsqrt_slow(a);
+}
+__device__ __forceinline__ double rcp_d(double a) {
+    return ff_in_range(a) ? rcp_d_core(a) : rcp_slow(a);
+}
+
 // Sign and ordering on the integer pipe (no FP64 instruction): negation and
 // absolute value flip / clear the sign bit of the high word; for doubles
 // >= 0 (and +0) the signed 64-bit patterns order like the values.
@@ -396,12 +407,18 @@ __device__ __forceinline__ double sqrt_hn(double a) {
     return __double_as_longlong(a) > 0 ? a * rsqrt_hn(a) : 0.0;
 }
 
-// Minimum image on a periodic axis: |d| > L/2 is tested on the bit patterns
-// (non-negative doubles order like their bits), so the test costs no FP64
-// instruction; d - sign(d) L equals the reference's (L - |d|) (+-1).
+// Minimum image on a periodic axis: |d| > L/2 is tested on the 32-bit words
+// of the bit patterns (non-negative doubles order like their bits; compared
+// as one 64-bit integer, the test is turned back into an FP64 compare), so
+// it costs no FP64 instruction; d - sign(d) L, the reference's (L - |d|)
+// (+-1), is a call: inlined it would be computed for every pair.
+static __device__ __noinline__ double wrap_slow(double d, double iv) {
+    return d - copysign(iv, d);
+}
 __device__ __forceinline__ double min_image(double d, double half_iv, double iv) {
-    const long long ad = __double_as_longlong(d) & 0x7fffffffffffffffLL;
-    if (ad > __double_as_longlong(half_iv)) d = d - copysign(iv, d);
+    const unsigned h = (unsigned)__double2hiint(d) & 0x7fffffffu, l = (unsigned)__double2loint(d);
+    const unsigned H = (unsigned)__double2hiint(half_iv), L = (unsigned)__double2loint(half_iv);
+    if (h > H || (h == H && l > L)) d = wrap_slow(d, iv);
     return d;
 }
 

@@ -39,6 +39,13 @@
 namespace cbg {
 
 #define CB_HD __host__ __device__ __forceinline__
+// Rare slow paths stay calls: inlined, the compiler computes them on every
+// call (predicated) and their FP64 instructions take FP64 issue slots.
+#ifdef __CUDACC__
+#define CB_SLOW static __host__ __device__ __noinline__
+#else
+#define CB_SLOW static __attribute__((noinline))
+#endif
 
 struct ff {
     float h, l;
@@ -309,6 +316,70 @@ CB_HD float ff_diff_f(ff a, ff b) {
     return ff_addr(s.h, ff_addr(s.l, ff_subr(a.l, b.l)));
 }
 
+// ------------------------------------------- FP64 results with few FP64 ops
+// For kernels bound by FP64 issue: full-precision FP64 results whose costly
+// parts run on the FP32 and integer pipes.
+
+// A double rounded toward zero to float (normal range), on the bit pattern.
+CB_HD float ff_f32(double x) {
+    const uint32_t hi = ff_dhi(x), lo = ff_dlo(x);
+    const int fe = (int)((hi >> 20) & 0x7ffu) - 896;
+    if (fe <= 0) return 0.0f;
+    return ff_bitsf((hi & 0x80000000u) | ((uint32_t)fe << 23) | ((hi & 0xfffffu) << 3) |
+                    (lo >> 29));
+}
+
+// y + c for a double y > 0 and a float c with |c| <= 2^-31 y: c in units of
+// the last place of y (below 2^22), rounded to an integer with the 1.5 * 2^23
+// shifter and added to y's bit pattern (error <= 1/2 ulp + 2^-7 ulp). The
+// FP64 sum when y's exponent is outside [-74, 178], c is larger, or the sum
+// leaves y's binade.
+CB_SLOW double ff_add_slow(double y, float c) { return y + (double)c; }
+CB_HD double ff_add_small(double y, float c) {
+    const uint32_t hi = ff_dhi(y), lo = ff_dlo(y);
+    const int se = 52 - ((int)((hi >> 20) & 0x7ffu) - 1023) + 127;  // 2^(52 - E)
+    const float u = ff_mulr(c, ff_bitsf((uint32_t)(se < 1 ? 1 : se > 254 ? 254 : se) << 23));
+    const int d = (int)(ff_fbits(ff_addr(u, 12582912.0f)) - 0x4b400000u);
+    const uint32_t lo2 = lo + (uint32_t)d;
+    const uint32_t hi2 = hi + (d < 0 ? 0xffffffffu : 0u) + (lo2 < lo ? 1u : 0u);
+    if (se < 1 || se > 254 || !(fabsf(u) < 4194304.0f) || ((hi2 ^ hi) & 0x7ff00000u))
+        return ff_add_slow(y, c);
+    return ff_mkd(hi2, lo2);
+}
+
+// true when a > 0 and float-float holds a, its root and reciprocal root
+CB_HD bool ff_in_range(double a) {
+    const int eb = (int)((ff_dhi(a) >> 20) & 0xfffu);  // sign bit included: a > 0 only
+    return eb > 1023 - 100 && eb < 1023 + 100;
+}
+
+// 1/sqrt(a) to ~1 ulp with 2 FP64 instructions, for ff_in_range(a): a
+// float-float estimate (~2^-46) widened to double, the residual
+// e = 1 - a y^2 in FP64, and the correction y e / 2 (~2^-46 y, needed to 8
+// bits) in FP32, added on the integer pipe.
+CB_HD double rsqrt_d_core(double a) {
+    const double y = ff_to_double(ff_rsqrt(ff_of(a)));
+    const double t = a * y;
+    const double e = fma(-t, y, 1.0);
+    return ff_add_small(y, ff_mulr(ff_mulr(0.5f, ff_f32(y)), ff_f32(e)));
+}
+
+// 1/a to ~1 ulp with 1 FP64 instruction (as rsqrt_d_core, e = 1 - a y).
+CB_HD double rcp_d_core(double a) {
+    const double y = ff_to_double(ff_rcp(ff_of(a)));
+    const double e = fma(-a, y, 1.0);
+    return ff_add_small(y, ff_mulr(ff_f32(y), ff_f32(e)));
+}
+
+// sqrt(a) in float-float (~2^-46 relative) rounded to double, no FP64
+// instruction; 0 for a <= 0; IEEE sqrt outside the float-float range.
+CB_SLOW double sqrt_slow(double a) { return a > 0.0 ? sqrt(a) : 0.0; }
+CB_HD double sqrt_ffd(double a) {
+    if (!ff_in_range(a)) return sqrt_slow(a);  // also a <= 0
+    return ff_to_double(ff_sqrt(ff_of(a)));
+}
+
 #undef CB_HD
+#undef CB_SLOW
 
 }  // namespace cbg

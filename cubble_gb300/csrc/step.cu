@@ -66,7 +66,7 @@ __device__ __forceinline__ void k_predict_body(const Bufs &b, const int vb, cons
         const double yp = fma(h, fma(3.0, V1[i], -O1[i]), Y[i]);
         double rp = R[i];
         if (gas) rp = fma(h, fma(3.0, V3[i], -O3[i]), rp);
-        const double inv = rcp_hn(rp);
+        const double inv = rcp_d(rp);
         const double rsq = rp * rp;
         if (b.ffr) st_rec(b.ffr, i, rp, inv, rsq);
         double4_32a p;
@@ -117,9 +117,11 @@ CB_KERNEL_PAIR((template <int DIM>), k_predict, (<DIM>), __launch_bounds__(kBloc
 //     ones (about 70 % of the listed pairs) in shared memory; the force and
 //     gas-exchange arithmetic (~23 FP64 instructions) then runs on full warps
 //     of overlapping pairs, not on warps with idle lanes;
-//   * minimum image by bit compare, 1/sqrt(m) and 1/(r1 + r2) by rsqrt_hn /
-//     rcp_hn, the division by m of the overlap formula as a product with
-//     (1/sqrt(m))^2, -w/4 on the exponent field;
+//   * minimum image by bit compare; 1/sqrt(m) and 1/(r1 + r2) to ~1 ulp by
+//     rsqrt_d / rcp_d (2 and 1 FP64 instructions, the rest on the FP32 and
+//     integer pipes); the division by m of the overlap formula as a product
+//     with (1/sqrt(m))^2; -w/4 on the exponent field; no product by f0 when
+//     it is 1;
 //   * contributions to both members go through FP64 reductions into the
 //     per-bubble accumulator rows.
 __device__ __forceinline__ void red_add(double *p, double v) {
@@ -167,8 +169,9 @@ __device__ __forceinline__ void k_pairs_body(const Bufs &b, const int vb, const 
         double *ai = b.acc + (size_t)i * kAcc;
         double *aj = b.acc + (size_t)j * kAcc;
         // velocity f0 d (1/|d| - 1/(r1 + r2)), src/kernels.cu:218-233
-        const double rs = rsqrt_hn(m);
-        const double s = f0 * (rs - rcp_hn(radii));
+        const double rs = rsqrt_d(m);
+        double s = rs - rcp_d(radii);
+        if (f0 != 1.0) s *= f0;
         const double fx = dx * s, fy = dy * s;
         red_add(ai + 0, fx);
         red_add(aj + 0, neg_bits(fx));
@@ -213,7 +216,8 @@ __device__ __forceinline__ void k_pairs_body(const Bufs &b, const int vb, const 
                     oa = 2.0 * min_nonneg(r1, r2);
                 } else {
                     const double wv = (r2sq - r1sq + m) * rs;
-                    oa = 2.0 * sqrt_hn(abs_bits(fma(neg_quarter(wv), wv, r2sq)));
+                    const double v = abs_bits(fma(neg_quarter(wv), wv, r2sq));
+                    oa = __double_as_longlong(v) > 0 ? 2.0 * (v * rsqrt_d(v)) : 0.0;
                 }
             }
             const double g = oa * (inv2 - inv1);
@@ -632,11 +636,18 @@ __device__ __forceinline__ void k_correct_body(const Bufs &b, const int vb, cons
             t = cz - S2[i];
             dist = fma(t, t, dist);
         }
-        dist = sqrt_hn2(dist);  // only its maximum over the foam is used
+        dist = sqrt_ffd(dist);  // ~2^-46; only its maximum over the foam is used
         int del = 0;
         if (gas) {  // mean-field gas exchange and radius, src/kernels.cu:390-431
-            const double inv = DIM == 3 ? b.invr[2 * (size_t)i] : p.w;
-            const double area = DIM == 3 ? (4.0 * kPi) * (rp * rp) : (2.0 * kPi) * rp;
+            double inv, area;
+            if (DIM == 3) {  // (1/rp, rp^2) record of k_predict
+                const double2 e = reinterpret_cast<const double2 *>(b.invr)[i];
+                inv = e.x;
+                area = (4.0 * kPi) * e.y;
+            } else {
+                inv = p.w;
+                area = (2.0 * kPi) * rp;
+            }
             double vr = mfa - inv;
             vr *= mfb * (area - ov);
             vr += vpr;
@@ -667,7 +678,7 @@ __device__ __forceinline__ void k_correct_body(const Bufs &b, const int vb, cons
                 t = z0 - cz;
                 d2 = fma(t, t, d2);
             }
-            PATHN[i] = PATH[i] + sqrt_hn2(d2);  // ~1e-13 relative per increment
+            PATHN[i] = PATH[i] + sqrt_ffd(d2);  // increment to ~2^-46
         }
         ERR[i] = __longlong_as_double(max(e, __double_as_longlong(ERR[i])));  // both >= 0
         merr = max(merr, e);

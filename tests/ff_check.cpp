@@ -34,7 +34,8 @@ int main() {
 
     Max split{"split"}, back{"to_double"}, back_ulp{"to_double_ulps"}, add{"add"},
         addc{"add_cancel_abs"}, mul{"mul"}, sqr{"sqr"}, rcp{"rcp"}, rsq{"rsqrt"},
-        sqt{"sqrt"}, pair{"pair_velocity"}, chord{"chord_area_abs"};
+        sqt{"sqrt"}, pair{"pair_velocity"}, chord{"chord_area_abs"}, rsqd{"rsqrt_d_ulps"},
+        rcpd{"rcp_d_ulps"}, sqd{"sqrt_ffd"}, small{"add_small_ulps"};
     const int N = 400000;
     for (int it = 0; it < N; it++) {
         // split: top 24 bits exact, the rest to 2^-47
@@ -69,6 +70,22 @@ int main() {
         rcp.add(rel(val(cbg::ff_rcp(p)), 1.0L / val(p)));
         rsq.add(rel(val(cbg::ff_rsqrt(p)), 1.0L / std::sqrt(val(p))));
         sqt.add(rel(val(cbg::ff_sqrt(p)), std::sqrt(val(p))));
+        // FP64 results with few FP64 instructions: 1/sqrt and 1/x to ~1 ulp
+        {
+            const double q = logu(-90, 90);
+            const double rd = cbg::rsqrt_d_core(q), cd = cbg::rcp_d_core(q);
+            const ld rq = 1.0L / std::sqrt((ld)q), cq = 1.0L / (ld)q;
+            rsqd.add((rd > rq ? rd - rq : rq - rd) / (ld)std::ldexp(1.0, std::ilogb(rd) - 52));
+            rcpd.add((cd > cq ? cd - cq : cq - cd) / (ld)std::ldexp(1.0, std::ilogb(cd) - 52));
+            sqd.add(rel((ld)cbg::sqrt_ffd(q), std::sqrt((ld)q)));
+            // y + c for |c| <= 2^-31 y, near binade edges too
+            double y = logu(-60, 60);
+            if (it % 5 == 0) y = std::ldexp(1.0, (int)(U(rng) * 100) - 50) * (1.0 + 1e-15 * sgn());
+            const float cc = (float)(sgn() * y * logu(-70, -31));
+            const double z = cbg::ff_add_small(y, cc);
+            const ld zq = (ld)y + (ld)cc;
+            small.add((z > zq ? z - zq : zq - z) / (ld)std::ldexp(1.0, std::ilogb(z) - 52));
+        }
         // the pair velocity factor f0 (1/|d| - 1/(r1 + r2)) and the chord
         // area r2^2 - w^2 / 4, w = (r2^2 - r1^2 + m) / |d|, on overlapping
         // pairs of radii ~ 1 (|d| < r1 + r2)
@@ -99,7 +116,7 @@ int main() {
         chord.add((val(oa) > oaL ? val(oa) - oaL : oaL - val(oa)) / scale);
     }
     for (Max *m : {&split, &back, &back_ulp, &add, &addc, &mul, &sqr, &rcp, &rsq, &sqt, &pair,
-                   &chord})
+                   &chord, &rsqd, &rcpd, &sqd, &small})
         std::printf("%s %.6Le\n", m->name, m->v);
     return 0;
 }

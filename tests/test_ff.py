@@ -6,7 +6,8 @@ to double is within half an ulp; sums, products, reciprocal, rsqrt and sqrt
 stay within 2^-45 relative; the pair velocity factor f0 (1/|d| - 1/(r1 + r2))
 within 2^-45 of 1/|d|; the chord area r2^2 - w^2 / 4 within 2^-45 of
 r1^2 + r2^2 + |d|^2. These bound the FP64 form's pair terms well inside its
-1e-12 parity bar."""
+1e-12 parity bar. The FP64 reciprocal and reciprocal square root built on
+them (one or two FP64 instructions) stay within 1 ulp."""
 import os
 import shutil
 import subprocess
@@ -37,6 +38,15 @@ def test_split_and_back(errors):
 
 
 @pytest.mark.parametrize("op", ["add", "add_cancel_abs", "mul", "sqr", "rcp", "rsqrt", "sqrt",
-                                "pair_velocity", "chord_area_abs"])
+                                "pair_velocity", "chord_area_abs", "sqrt_ffd"])
 def test_operations(errors, op):
     assert errors[op] <= 2.0 ** -45, (op, errors[op])
+
+
+def test_fp64_results_with_few_fp64_instructions(errors):
+    """1/sqrt and 1/x of the FP64 kernels (float-float estimate, one FP64
+    residual, the correction added on the integer pipe): within 1 ulp; the
+    small addition within 1/2 ulp plus its FP32 rounding."""
+    assert errors["rsqrt_d_ulps"] <= 1.0
+    assert errors["rcp_d_ulps"] <= 1.0
+    assert errors["add_small_ulps"] <= 0.51
