@@ -128,12 +128,14 @@ __device__ __forceinline__ void red_add(double *p, double v) {
     asm volatile("red.global.add.f64 [%0], %1;" ::"l"(p), "d"(v));
 }
 // -w/4, exact: the exponent field lowered by 2 and the sign flipped when the
-// exponent allows it (|w| > 2^-1020), else the FP64 product.
+// exponent allows it (|w| > 2^-1020), else the FP64 product (a call, so that
+// it is not computed for every pair).
+static __device__ __noinline__ double neg_quarter_slow(double w) { return -0.25 * w; }
 __device__ __forceinline__ double neg_quarter(double w) {
     const int hi = __double2hiint(w);
     if ((hi & 0x7ff00000) > 0x00200000)
         return __hiloint2double((hi - 0x00200000) ^ (int)0x80000000, __double2loint(w));
-    return -0.25 * w;
+    return neg_quarter_slow(w);
 }
 
 constexpr int kQueue = 64;  // per-warp queue of overlapping pairs
@@ -529,6 +531,82 @@ __device__ __forceinline__ bool touches_wall(double f0, double rad, double x, do
     return false;
 }
 
+// Flow, shear and wall terms of the velocity (addFlowVelocity,
+// addWallVelocity, src/kernels.cu:497-593) as a call taken only when one of
+// them is on: inlined, their FP64 arithmetic would be predicated into every
+// bubble's path and take FP64 issue slots.
+struct Vel3 {
+    double x, y, z;
+};
+template <int DIM>
+static __device__ __noinline__ Vel3 boundary_velocity(const DevConst &k, int flow, int shear,
+                                                      double drag, double vpx, double vpy,
+                                                      double vpz, double xp, double yp, double zp,
+                                                      double rp, double f0, double f1, double f2,
+                                                      int nn) {
+    if (flow) {  // addFlowVelocity, src/kernels.cu:497-544
+        double multiplier = nn;
+        multiplier = (multiplier > 0 ? 1.0 / multiplier : 0.0);
+        const double riSq = rp * rp;
+        int inside = (int)((xp < k.flow_tfr[0] && xp > k.flow_lbb[0]) ||
+                           ((k.flow_lbb[0] - xp) * (k.flow_lbb[0] - xp) <= riSq) ||
+                           ((k.flow_tfr[0] - xp) * (k.flow_tfr[0] - xp) <= riSq));
+        inside *= (int)((yp < k.flow_tfr[1] && yp > k.flow_lbb[1]) ||
+                        ((k.flow_lbb[1] - yp) * (k.flow_lbb[1] - yp) <= riSq) ||
+                        ((k.flow_tfr[1] - yp) * (k.flow_tfr[1] - yp) <= riSq));
+        if (DIM == 3) {
+            inside *= (int)((zp < k.flow_tfr[2] && zp > k.flow_lbb[2]) ||
+                            ((k.flow_lbb[2] - zp) * (k.flow_lbb[2] - zp) <= riSq) ||
+                            ((k.flow_tfr[2] - zp) * (k.flow_tfr[2] - zp) <= riSq));
+            vpz += !inside * multiplier * f2 + k.flow_vel[2] * inside;
+        }
+        vpx += !inside * multiplier * f0 + k.flow_vel[0] * inside;
+        vpy += !inside * multiplier * f1 + k.flow_vel[1] * inside;
+    }
+    if (shear) {  // linear shear along x over the last axis (cb_config.shear_speed)
+        const double q = DIM == 3 ? zp : yp;
+        vpx += k.shear * ((q - k.lbb[DIM - 1]) * k.shear_il - 1.0);
+    }
+    if (k.any_wall) {  // addWallVelocity, src/kernels.cu:546-593
+        double xDrag = 1.0, yDrag = 1.0, velocity = 0.0;
+        if (k.wall[0] && touches_wall(k.f0, rp, xp, k.lbb[0], k.tfr[0], velocity)) {
+            vpx += velocity;
+            vpy *= drag;
+            vpz *= drag;
+            xDrag = drag;
+        }
+        velocity = 0.0;
+        if (k.wall[1] && touches_wall(k.f0, rp, yp, k.lbb[1], k.tfr[1], velocity)) {
+            vpx *= drag;
+            vpy += velocity * xDrag;
+            vpz *= drag;
+            yDrag = drag;
+        }
+        velocity = 0.0;
+        if (k.wall[2] && touches_wall(k.f0, rp, zp, k.lbb[2], k.tfr[2], velocity)) {
+            vpx *= drag;
+            vpy *= drag;
+            vpz += velocity * xDrag * yDrag;
+        }
+    }
+    return {vpx, vpy, vpz};
+}
+
+// |(a, b, c)| of exact FP64 differences of nearby positions: squares, sum
+// and root in float-float (~2^-46), no FP64 instruction.
+static __device__ __noinline__ double norm_slow(double s) { return s > 0.0 ? sqrt(s) : 0.0; }
+template <int DIM>
+__device__ __forceinline__ double norm_ffd(double a, double b, double c) {
+    ff s = ff_add(ff_sqr(ff_of(a)), ff_sqr(ff_of(b)));
+    if (DIM == 3) s = ff_add(s, ff_sqr(ff_of(c)));
+    if (!(s.h > 0x1p-100f && s.h < 0x1p100f)) {
+        double d = a * a + b * b;
+        if (DIM == 3) d += c * c;
+        return norm_slow(d);
+    }
+    return ff_to_double(ff_sqrt(s));
+}
+
 template <int DIM>
 __device__ __forceinline__ void k_correct_body(const Bufs &b, const int vb, const int vg) {
     __shared__ double smem[32];
@@ -571,72 +649,30 @@ __device__ __forceinline__ void k_correct_body(const Bufs &b, const int vb, cons
         const double ov = a1.x;
         const double4_32a p = ld4(b.pred, i);
         const double xp = p.x, yp = p.y, zp = DIM == 3 ? p.z : 0.0, rp = DIM == 3 ? p.w : p.z;
-        if (flow) {  // addFlowVelocity, src/kernels.cu:497-544
-            double multiplier = NN[i];
-            multiplier = (multiplier > 0 ? 1.0 / multiplier : 0.0);
-            const double riSq = rp * rp;
-            int inside = (int)((xp < k.flow_tfr[0] && xp > k.flow_lbb[0]) ||
-                               ((k.flow_lbb[0] - xp) * (k.flow_lbb[0] - xp) <= riSq) ||
-                               ((k.flow_tfr[0] - xp) * (k.flow_tfr[0] - xp) <= riSq));
-            inside *= (int)((yp < k.flow_tfr[1] && yp > k.flow_lbb[1]) ||
-                            ((k.flow_lbb[1] - yp) * (k.flow_lbb[1] - yp) <= riSq) ||
-                            ((k.flow_tfr[1] - yp) * (k.flow_tfr[1] - yp) <= riSq));
-            if (DIM == 3) {
-                inside *= (int)((zp < k.flow_tfr[2] && zp > k.flow_lbb[2]) ||
-                                ((k.flow_lbb[2] - zp) * (k.flow_lbb[2] - zp) <= riSq) ||
-                                ((k.flow_tfr[2] - zp) * (k.flow_tfr[2] - zp) <= riSq));
-                vpz += !inside * multiplier * a1.w + k.flow_vel[2] * inside;
-            }
-            vpx += !inside * multiplier * a1.y + k.flow_vel[0] * inside;
-            vpy += !inside * multiplier * a1.z + k.flow_vel[1] * inside;
-        }
-        if (shear) {  // linear shear along x over the last axis (cb_config.shear_speed)
-            const double q = DIM == 3 ? zp : yp;
-            vpx += k.shear * ((q - k.lbb[DIM - 1]) * k.shear_il - 1.0);
-        }
-        if (k.any_wall) {  // addWallVelocity, src/kernels.cu:546-593
-            double xDrag = 1.0, yDrag = 1.0, velocity = 0.0;
-            if (k.wall[0] && touches_wall(k.f0, rp, xp, k.lbb[0], k.tfr[0], velocity)) {
-                vpx += velocity;
-                vpy *= drag;
-                vpz *= drag;
-                xDrag = drag;
-            }
-            velocity = 0.0;
-            if (k.wall[1] && touches_wall(k.f0, rp, yp, k.lbb[1], k.tfr[1], velocity)) {
-                vpx *= drag;
-                vpy += velocity * xDrag;
-                vpz *= drag;
-                yDrag = drag;
-            }
-            velocity = 0.0;
-            if (k.wall[2] && touches_wall(k.f0, rp, zp, k.lbb[2], k.tfr[2], velocity)) {
-                vpx *= drag;
-                vpy *= drag;
-                vpz += velocity * xDrag * yDrag;
-            }
+        if (flow | shear | k.any_wall) {
+            const Vel3 v = boundary_velocity<DIM>(k, flow, shear, drag, vpx, vpy, vpz, xp, yp, zp,
+                                                  rp, a1.y, a1.z, a1.w, flow ? NN[i] : 0);
+            vpx = v.x;
+            vpy = v.y;
+            vpz = v.z;
         }
         // AM2 correct x + 0.5 ts (v + vp), src/kernels.cu:487-495 and :366-387
         long long e = 0;
-        double t, dist;
         const double x0 = X[i], y0 = Y[i];
         const double cx = fma(h, V0[i] + vpx, x0);
         e = max_bits(e, abs_bits(xp - cx));
-        t = cx - S0[i];
-        dist = t * t;
         const double cy = fma(h, V1[i] + vpy, y0);
         e = max_bits(e, abs_bits(yp - cy));
-        t = cy - S1[i];
-        dist = fma(t, t, dist);
-        double cz = 0.0, z0 = 0.0;
+        double cz = 0.0, z0 = 0.0, sz = 0.0;
         if (DIM == 3) {
             z0 = Z[i];
             cz = fma(h, V2[i] + vpz, z0);
             e = max_bits(e, abs_bits(zp - cz));
-            t = cz - S2[i];
-            dist = fma(t, t, dist);
+            sz = cz - S2[i];
         }
-        dist = sqrt_ffd(dist);  // ~2^-46; only its maximum over the foam is used
+        // distance from the position of the last search; only its maximum
+        // over the foam is used (the search trigger)
+        double dist = norm_ffd<DIM>(cx - S0[i], cy - S1[i], sz);
         int del = 0;
         if (gas) {  // mean-field gas exchange and radius, src/kernels.cu:390-431
             double inv, area;
@@ -669,17 +705,8 @@ __device__ __forceinline__ void k_correct_body(const Bufs &b, const int vb, cons
         }
         b.delflag[i] = del;
         mexp = max_bits(mexp, dist);
-        if (path) {  // src/kernels.cu:437-451
-            t = x0 - cx;
-            double d2 = t * t;
-            t = y0 - cy;
-            d2 = fma(t, t, d2);
-            if (DIM == 3) {
-                t = z0 - cz;
-                d2 = fma(t, t, d2);
-            }
-            PATHN[i] = PATH[i] + sqrt_ffd(d2);  // increment to ~2^-46
-        }
+        if (path)  // src/kernels.cu:437-451; the increment to ~2^-46
+            PATHN[i] = PATH[i] + norm_ffd<DIM>(x0 - cx, y0 - cy, z0 - cz);
         ERR[i] = __longlong_as_double(max(e, __double_as_longlong(ERR[i])));  // both >= 0
         merr = max(merr, e);
         XN[i] = cx;
