@@ -112,11 +112,12 @@ CB_KERNEL_PAIR((template <int DIM>), k_predict, (<DIM>), __launch_bounds__(kBloc
 // Overlap velocities, pairwise gas flux and overlap areas in FP64
 // (pairwiseInteraction, src/kernels.cu:172-337). FP64-issue bound on GB300
 // (2 FP64 thread-instructions per SM and cycle), so:
-//   * each warp takes 32 consecutive pairs, computes their FP64 geometry and
-//     overlap test (8 FP64 instructions a pair), and queues the overlapping
-//     ones (about 70 % of the listed pairs) in shared memory; the force and
-//     gas-exchange arithmetic (~23 FP64 instructions) then runs on full warps
-//     of overlapping pairs, not on warps with idle lanes;
+//   * each warp takes 32 consecutive pairs, computes their FP64 differences
+//     and overlap test (3 FP64 instructions a pair; the test in FP32 with a
+//     guard band), and queues the overlapping ones (about 70 % of the listed
+//     pairs) in shared memory; the distance, force and gas-exchange
+//     arithmetic then runs on full warps of overlapping pairs, not on warps
+//     with idle lanes;
 //   * minimum image by bit compare; 1/sqrt(m) and 1/(r1 + r2) to ~1 ulp by
 //     rsqrt_d / rcp_d (2 and 1 FP64 instructions, the rest on the FP32 and
 //     integer pipes); the division by m of the overlap formula as a product
@@ -140,12 +141,25 @@ __device__ __forceinline__ double neg_quarter(double w) {
 
 constexpr int kQueue = 64;  // per-warp queue of overlapping pairs
 
+// The overlap test of the reference in FP64 (the sign of the exact
+// (r1 + r2)^2 - m), for pairs in the FP32 guard band.
+template <int DIM>
+static __device__ __noinline__ bool overlap_exact(double dx, double dy, double dz, double r1,
+                                                  double r2) {
+    double m = dx * dx;
+    m = fma(dy, dy, m);
+    if (DIM == 3) m = fma(dz, dz, m);
+    const double radii = r1 + r2;
+    return nonneg_bits(fma(radii, radii, -m));
+}
+
 template <int DIM, bool GAS, bool FLOW>
 __device__ __forceinline__ void k_pairs_body(const Bufs &b, const int vb, const int vg) {
     constexpr int kW = kBlock / 32;
     __shared__ double smem[32];
-    // queue slots: dx, dy, dz (2D: r1), m, r1 + r2, (2D: r2)
-    __shared__ double qd[kW][DIM == 3 ? 5 : 6][kQueue];
+    // queue slots: dx, dy, (3D: dz), r1, r2
+    constexpr int kR1 = DIM == 3 ? 3 : 2, kSlots = kR1 + 2;
+    __shared__ double qd[kW][kSlots][kQueue];
     __shared__ int qij[kW][2][kQueue];
     const Ctrl *c = b.ctrl;
     const DevConst &k = *b.k;
@@ -166,8 +180,12 @@ __device__ __forceinline__ void k_pairs_body(const Bufs &b, const int vb, const 
     // the force and gas-exchange terms of queued (overlapping) pair e
     auto process = [&](int e) {
         const int i = QI[e], j = QJ[e];
-        const double dx = Q[0][e], dy = Q[1][e], m = Q[3][e], radii = Q[4][e];
-        const double dz = DIM == 3 ? Q[2][e] : 0.0;
+        const double dx = Q[0][e], dy = Q[1][e], dz = DIM == 3 ? Q[2][e] : 0.0;
+        const double r1 = Q[kR1][e], r2 = Q[kR1 + 1][e];
+        double m = dx * dx;
+        m = fma(dy, dy, m);
+        if (DIM == 3) m = fma(dz, dz, m);
+        const double radii = r1 + r2;
         double *ai = b.acc + (size_t)i * kAcc;
         double *aj = b.acc + (size_t)j * kAcc;
         // velocity f0 d (1/|d| - 1/(r1 + r2)), src/kernels.cu:218-233
@@ -185,7 +203,7 @@ __device__ __forceinline__ void k_pairs_body(const Bufs &b, const int vb, const 
             red_add(aj + 2, neg_bits(fz));
         }
         if (GAS) {  // pairwise gas exchange, src/kernels.cu:236-280
-            double r1sq, r2sq, inv1, inv2, r1 = 0.0, r2 = 0.0;
+            double r1sq, r2sq, inv1, inv2;
             if (DIM == 3) {  // (1/r, r^2) records written by k_predict
                 const double2 e1 = reinterpret_cast<const double2 *>(b.invr)[i];
                 const double2 e2 = reinterpret_cast<const double2 *>(b.invr)[j];
@@ -194,8 +212,6 @@ __device__ __forceinline__ void k_pairs_body(const Bufs &b, const int vb, const 
                 inv2 = e2.x;
                 r2sq = e2.y;
             } else {
-                r1 = Q[2][e];
-                r2 = Q[5][e];
                 r1sq = r1 * r1;
                 r2sq = r2 * r2;
                 inv1 = b.pred[4 * (size_t)i + 3];
@@ -243,7 +259,7 @@ __device__ __forceinline__ void k_pairs_body(const Bufs &b, const int vb, const 
         const int p = (ch << 5) + lane;
         bool over = false;
         int i = 0, j = 0;
-        double dx = 0.0, dy = 0.0, dz = 0.0, m = 0.0, radii = 0.0, r1 = 0.0, r2 = 0.0;
+        double dx = 0.0, dy = 0.0, dz = 0.0, r1 = 0.0, r2 = 0.0;
         if (p < np) {
             i = PI[p];
             j = PJ[p];
@@ -265,12 +281,19 @@ __device__ __forceinline__ void k_pairs_body(const Bufs &b, const int vb, const 
                 dz = a.z - q.z;
                 if (pz) dz = min_image(dz, hz, Lz);
             }
-            m = dx * dx;
-            m = fma(dy, dy, m);
-            if (DIM == 3) m = fma(dz, dz, m);
-            radii = r1 + r2;
-            // overlap test radii^2 >= m on the sign of the exact difference
-            over = nonneg_bits(fma(radii, radii, -m));
+            // overlap test (r1 + r2)^2 >= m: in FP32 on the exact differences
+            // (truncated, ~2^-21 relative) outside a 1e-5 guard band, by the
+            // FP64 test of the reference's sign inside it
+            const float fx = ff_f32(dx), fy = ff_f32(dy), fz = DIM == 3 ? ff_f32(dz) : 0.f;
+            float m32 = fx * fx;
+            m32 = fmaf(fy, fy, m32);
+            if (DIM == 3) m32 = fmaf(fz, fz, m32);
+            const float R32 = ff_f32(r1) + ff_f32(r2);
+            const float RR = R32 * R32;
+            if (m32 < RR * (1.f - 1e-5f))
+                over = true;
+            else if (!(m32 > RR * (1.f + 1e-5f)))
+                over = overlap_exact<DIM>(dx, dy, dz, r1, r2);
         }
         const unsigned mask = __ballot_sync(0xffffffffu, over);
         if (over) {
@@ -279,10 +302,9 @@ __device__ __forceinline__ void k_pairs_body(const Bufs &b, const int vb, const 
             QJ[e] = j;
             Q[0][e] = dx;
             Q[1][e] = dy;
-            Q[2][e] = DIM == 3 ? dz : r1;
-            Q[3][e] = m;
-            Q[4][e] = radii;
-            if (DIM == 2) Q[5][e] = r2;
+            if (DIM == 3) Q[2][e] = dz;
+            Q[kR1][e] = r1;
+            Q[kR1 + 1][e] = r2;
         }
         cnt += __popc(mask);
         __syncwarp();
@@ -294,7 +316,7 @@ __device__ __forceinline__ void k_pairs_body(const Bufs &b, const int vb, const 
                 QI[lane] = QI[32 + lane];
                 QJ[lane] = QJ[32 + lane];
 #pragma unroll
-                for (int t = 0; t < (DIM == 3 ? 5 : 6); t++) Q[t][lane] = Q[t][32 + lane];
+                for (int t = 0; t < kSlots; t++) Q[t][lane] = Q[t][32 + lane];
             }
             __syncwarp();
         }
