@@ -680,6 +680,9 @@ __device__ __forceinline__ void k_correct_body(const Bufs &b, const int vb, cons
         }
         // AM2 correct x + 0.5 ts (v + vp), src/kernels.cu:487-495 and :366-387
         long long e = 0;
+        // inputs read after the first store below, loaded up front (a load
+        // cannot move across a store the compiler thinks may alias it)
+        const double err0 = ERR[i], path0 = path ? PATH[i] : 0.0;
         const double x0 = X[i], y0 = Y[i];
         const double cx = fma(h, V0[i] + vpx, x0);
         e = max_bits(e, abs_bits(xp - cx));
@@ -728,8 +731,8 @@ __device__ __forceinline__ void k_correct_body(const Bufs &b, const int vb, cons
         b.delflag[i] = del;
         mexp = max_bits(mexp, dist);
         if (path)  // src/kernels.cu:437-451; the increment to ~2^-46
-            PATHN[i] = PATH[i] + norm_ffd<DIM>(x0 - cx, y0 - cy, z0 - cz);
-        ERR[i] = __longlong_as_double(max(e, __double_as_longlong(ERR[i])));  // both >= 0
+            PATHN[i] = path0 + norm_ffd<DIM>(x0 - cx, y0 - cy, z0 - cz);
+        ERR[i] = __longlong_as_double(max(e, __double_as_longlong(err0)));  // both >= 0
         merr = max(merr, e);
         XN[i] = cx;
         YN[i] = cy;

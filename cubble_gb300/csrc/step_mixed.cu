@@ -512,6 +512,13 @@ __device__ __forceinline__ void k_correct_mx_body(const Bufs &b, const int vb, c
         const float ox = CB_F(RVO0)[i], oy = CB_F(RVO1)[i], oz = DIM == 3 ? CB_F(RVO2)[i] : 0.f;
         const double x0 = CB_D(RX)[i], y0 = CB_D(RY)[i], z0 = DIM == 3 ? CB_D(RZ)[i] : 0.0;
         const double r0 = CB_D(RR)[i];
+        // every other input up front, before the first store: the compiler
+        // cannot move a load across a store it may alias, and loads issued
+        // late leave their latency exposed
+        const double s0 = CB_D(RS0)[i], s1 = CB_D(RS1)[i], s2 = DIM == 3 ? CB_D(RS2)[i] : 0.0;
+        const double s3 = GAS ? CB_D(RS3)[i] : 0.0;
+        const double err0 = CB_D(RERR)[i];
+        const double path0 = path ? CB_D(RPATH)[i] : 0.0;
         float vr = 0.f, or_ = 0.f;
         float rp = float_from_double(r0);
         if (GAS) {
@@ -585,9 +592,9 @@ __device__ __forceinline__ void k_correct_mx_body(const Bufs &b, const int vb, c
         float e = fmaxf(fabsf(fmaf(2.f, vx, -ox) - vpx), fabsf(fmaf(2.f, vy, -oy) - vpy));
         if (DIM == 3) e = fmaxf(e, fabsf(fmaf(2.f, vz, -oz) - vpz));
         // expansion since the last search, src/kernels.cu:366-387
-        const float dx = float_from_double(cx - CB_D(RS0)[i]);
-        const float dy = float_from_double(cy - CB_D(RS1)[i]);
-        const float dz = DIM == 3 ? float_from_double(cz - CB_D(RS2)[i]) : 0.f;
+        const float dx = float_from_double(cx - s0);
+        const float dy = float_from_double(cy - s1);
+        const float dz = DIM == 3 ? float_from_double(cz - s2) : 0.f;
         float dist = sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
         int del = 0;
         double cr_keep = r0;
@@ -601,7 +608,7 @@ __device__ __forceinline__ void k_correct_mx_body(const Bufs &b, const int vb, c
             const double cr = r0 + double_from_float(ir);
             cr_keep = cr;
             e = fmaxf(e, fabsf(fmaf(2.f, vr, -or_) - w));
-            dist += float_from_double(cr - CB_D(RS3)[i]);
+            dist += float_from_double(cr - s3);
             if (__double_as_longlong(cr) > minr) {
                 vol = fma(DIM == 3 ? cr * cr : cr, cr, vol);  // sum of r^D
             } else {
@@ -617,10 +624,9 @@ __device__ __forceinline__ void k_correct_mx_body(const Bufs &b, const int vb, c
         mexp = fmaxf(mexp, dist);
         const double ed = double_from_float(h * e);
         merr = max(merr, __double_as_longlong(ed));
-        double *ERR = CB_D(RERR);
-        ERR[i] = __longlong_as_double(max(__double_as_longlong(ERR[i]), __double_as_longlong(ed)));
+        CB_D(RERR)[i] = __longlong_as_double(max(__double_as_longlong(err0), __double_as_longlong(ed)));
         if (path) {  // src/kernels.cu:437-451
-            CB_D(RPATHN)[i] = CB_D(RPATH)[i] +
+            CB_D(RPATHN)[i] = path0 +
                               double_from_float(sqrtf(fmaf(iz, iz, fmaf(iy, iy, ix * ix))));
         }
         CB_D(RXN)[i] = cx;
