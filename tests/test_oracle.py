@@ -260,3 +260,41 @@ def test_oracle_shear_profile():
     expect = 0.05 * (2.0 * z / L - 1.0)
     np.testing.assert_allclose(a["dxdtp"], expect, rtol=1e-12, atol=1e-15)
     np.testing.assert_allclose(a["dydtp"], 0.0, atol=1e-15)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_degenerate_foams(oracle_mod, dim):
+    """No bubbles, one bubble, two overlapping and two apart: the step runs,
+    a lone bubble stays where it is, an overlapping pair separates
+    symmetrically and the gas volume is unchanged."""
+    import cubble_gb300 as cb
+    from cubble_gb300 import workloads
+    for n, overlap in ((0, True), (1, True), (2, True), (2, False)):
+        cfg, st = workloads.foam(4, dim, 0.5, seed=3)
+        cfg.lbb = cb._abi.D3(0.0, 0.0, 0.0)
+        cfg.tfr = cb._abi.D3(10.0, 10.0, 10.0 if dim == 3 else 0.0)
+        st = {k: np.asarray(v)[:n].copy() for k, v in st.items()}
+        if n:
+            st["x"][:] = [4.0, 5.5][:n]
+            st["y"][:] = 5.0
+            st["r"][:] = 1.0
+            if dim == 3:
+                st["z"][:] = 5.0
+            if n == 2 and not overlap:
+                st["x"][1] = 7.5
+            st["index"] = np.arange(n, dtype=np.int32)
+        o = oracle_mod.OracleFoam(cfg)
+        o.load_state(st)
+        workloads.prepare(o)
+        v0 = o.total_volume()
+        r = o.integrate(5)
+        assert r["status"] == 0 and r["steps"] == 5 and r["count"] == n
+        s = o.get_state()
+        if n == 1:
+            assert s["x"][0] == 4.0
+        if n == 2:
+            assert r["num_pairs"] == 1 if overlap else True
+            if overlap:
+                assert s["x"][0] < 4.0 and s["x"][1] > 5.5
+                assert s["x"][0] - 4.0 == pytest.approx(-(s["x"][1] - 5.5), rel=1e-12)
+        assert o.total_volume() == pytest.approx(v0, rel=1e-12, abs=1e-300)
