@@ -76,6 +76,9 @@ struct DevConst {
     int mixed;
     float f0_f;  // f0/mu0 as FP32
     float f0_l;  // f0/mu0 - f0_f: the float-float f0 of k_pairs_ff
+    // FP32 copies for the search's candidate tests (a double -> float
+    // conversion is an FP64-pipe instruction)
+    float skin_f, lbb_f[3];
     int ffpair;  // CB_PRECISION_FP64_FF: pair terms in float-float
     float kq_f;  // K / (4 pi) in 3D, K / (2 pi) in 2D, as FP32
     float pre_margin;  // FP32 pair-search prefilter margin (length units)

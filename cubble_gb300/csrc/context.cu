@@ -80,6 +80,8 @@ void fill_const(cb_context *c) {
     k.ffpair = f.precision == CB_PRECISION_FP64_FF ? 1 : 0;
     k.f0_f = (float)k.f0;
     k.f0_l = (float)(k.f0 - (double)k.f0_f);
+    k.skin_f = (float)k.skin;
+    for (int a = 0; a < 3; a++) k.lbb_f[a] = (float)k.lbb[a];
     k.kq_f = (float)(k.dim == 3 ? k.K / (4.0 * 3.1415926535897932384626433832795) :
                                   k.K / (2.0 * 3.1415926535897932384626433832795));
     for (int a = 0; a < 3; a++) {

@@ -311,13 +311,22 @@ constexpr int kWarpsPerBlock = kBlock / 32;
 
 // Is j a pair partner of i (comparePair, src/kernels.cu:619-623)? Decided in
 // FP32 unless the distance lies within the guard band `pre_margin` of the
-// cutoff; there the reference's exact FP64 test decides (i's FP64 position
-// is loaded once, on first need, into xi..ri).
+// cutoff; there the reference's exact FP64 test decides. That test is a
+// call: inlined, its FP64 loads and arithmetic are predicated into every
+// candidate and take FP64 issue slots.
+template <int DIM>
+static __device__ __noinline__ bool pair_take_exact(const DevConst &k, int i, int j,
+                                                    const double *X, const double *Y,
+                                                    const double *Z, const double *R) {
+    const double maxd = __dadd_rn(__dadd_rn(R[i], R[j]), k.skin);
+    const double sq = exact_sqdist<DIM>(k, X[i], Y[i], DIM == 3 ? Z[i] : 0.0, X[j], Y[j],
+                                        DIM == 3 ? Z[j] : 0.0);
+    return sq < __dmul_rn(maxd, maxd);
+}
 template <int DIM>
 __device__ __forceinline__ bool pair_take(const DevConst &k, const float4 &pi, const float4 &pj,
                                           int i, int j, const double *X, const double *Y,
-                                          const double *Z, const double *R, double &xi,
-                                          double &yi, double &zi, double &ri) {
+                                          const double *Z, const double *R) {
     const bool per[3] = {!k.wall[0], !k.wall[1], !k.wall[2]};
     float dx = fabsf(pi.x - pj.x), dy = fabsf(pi.y - pj.y);
     float dz = DIM == 3 ? fabsf(pi.z - pj.z) : 0.f;
@@ -326,20 +335,12 @@ __device__ __forceinline__ bool pair_take(const DevConst &k, const float4 &pi, c
     if (DIM == 3 && per[2] && dz > k.half_iv32[2]) dz = k.iv32[2] - dz;
     float d2 = fmaf(dx, dx, dy * dy);
     if (DIM == 3) d2 = fmaf(dz, dz, d2);
-    const float cut = pi.w + pj.w + (float)k.skin;
+    const float cut = pi.w + pj.w + k.skin_f;
     const float band = k.pre_margin;
     const float hi = cut + band, lo = fmaxf(cut - band, 0.f);
     if (d2 >= hi * hi) return false;
     if (d2 < lo * lo) return true;
-    if (ri == 0.0) {
-        xi = X[i];
-        yi = Y[i];
-        zi = DIM == 3 ? Z[i] : 0.0;
-        ri = R[i];
-    }
-    const double maxd = __dadd_rn(__dadd_rn(ri, R[j]), k.skin);
-    const double sq = exact_sqdist<DIM>(k, xi, yi, zi, X[j], Y[j], DIM == 3 ? Z[j] : 0.0);
-    return sq < __dmul_rn(maxd, maxd);
+    return pair_take_exact<DIM>(k, i, j, X, Y, Z, R);
 }
 
 // Pair rows of one cell per warp: lanes are the cell's bubbles (32 at a
@@ -381,7 +382,6 @@ __device__ __forceinline__ void k_pair_cells_body(const Bufs &b, const int vb, c
             const int i = h0 + lane;
             const bool active = i < e0;
             float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
-            double xi = 0.0, yi = 0.0, zi = 0.0, ri = 0.0;
             int base = 0, cnt = 0;
             if (active) {
                 pi = b.pos32[i];
@@ -399,7 +399,7 @@ __device__ __forceinline__ void k_pair_cells_body(const Bufs &b, const int vb, c
                         const int j = c0 + t;
                         const float4 pj = stage[w][t];
                         if (!active || j <= i) continue;
-                        const bool take = pair_take<DIM>(k, pi, pj, i, j, X, Y, Z, R, xi, yi, zi, ri);
+                        const bool take = pair_take<DIM>(k, pi, pj, i, j, X, Y, Z, R);
                         if (take) {
                             if (WRITE && base + cnt < pcap) {
                                 PI[base + cnt] = i;
@@ -462,14 +462,14 @@ __device__ __forceinline__ void k_pair_rows_body(const Bufs &b, const int vb, co
     float cw[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) cw[a] = k.iv32[a] / (float)cd[a];
-    const float reach0 = c->search_maxr + (float)k.skin + k.pre_margin + 1e-3f;
+    const float reach0 = c->search_maxr + k.skin_f + k.pre_margin + 1e-3f;
     bool over = false;
     for (int i = vb * blockDim.x + threadIdx.x; i < n; i += vg * blockDim.x) {
         const int cell = b.cellSorted[i];
         const int kk[3] = {cell % cd[0], (cell / cd[0]) % cd[1], cell / (cd[0] * cd[1])};
         const float4 pi = b.pos32[i];
-        const float pr[3] = {pi.x - (float)k.lbb[0], pi.y - (float)k.lbb[1],
-                             DIM == 3 ? pi.z - (float)k.lbb[2] : 0.f};
+        const float pr[3] = {pi.x - k.lbb_f[0], pi.y - k.lbb_f[1],
+                             DIM == 3 ? pi.z - k.lbb_f[2] : 0.f};
         const float reach = pi.w + reach0;
         // distance from the bubble to the lower / upper face of its cell
         float lo[3], hi[3];
@@ -522,13 +522,12 @@ __device__ __forceinline__ void k_pair_rows_body(const Bufs &b, const int vb, co
             }
             nb[p] = v;
         }
-        double xi = 0.0, yi = 0.0, zi = 0.0, ri = 0.0;
         int cnt = 0;
         for (int t = 0; t < nq; t++) {
             const int qc = nb[t];
             const int ce = b.cellStart[qc + 1];
             for (int j = max(b.cellStart[qc], i + 1); j < ce; j++) {
-                if (pair_take<DIM>(k, pi, b.pos32[j], i, j, X, Y, Z, R, xi, yi, zi, ri)) {
+                if (pair_take<DIM>(k, pi, b.pos32[j], i, j, X, Y, Z, R)) {
                     if (cnt < M) b.stash[(size_t)i * M + cnt] = j;
                     cnt++;
                 }
