@@ -87,6 +87,22 @@ def test_cli_mixed_form_and_3d(tmp_path):
     assert len(results(tmp)) >= 1
 
 
+def test_cli_fp64_ff_form_matches_fp64(tmp_path):
+    """--precision fp64_ff (pair terms in float-float) against the default
+    FP64 form on the same input: the first printed rows agree to 1e-9."""
+    rows = {}
+    for form in ("fp64", "fp64_ff"):
+        tmp = os.path.join(str(tmp_path), form)
+        os.makedirs(tmp)
+        out = run_cli(tmp, ["input.json", "--max-steps", "800", "--precision", form],
+                      small_input())
+        assert ("%s form" % form) in out
+        rows[form] = results(tmp)
+    k = min(len(rows["fp64"]), len(rows["fp64_ff"]), 2)
+    assert k >= 1
+    np.testing.assert_allclose(rows["fp64_ff"][:k], rows["fp64"][:k], rtol=1e-9, atol=1e-12)
+
+
 def test_cli_walls_and_shear_3d(tmp_path):
     """3D with walls in z and the linear shear extension (the large sheared
     foam's setting), mixed form: runs, writes finite rows, and the mean x
