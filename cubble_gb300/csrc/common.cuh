@@ -572,8 +572,11 @@ __device__ void finish_attempt(Ctrl *c, const DevConst &k, double fErr, double f
         const int accepted = !too_large;
         set_cond(c->h_delete, ok && accepted && c->need_delete);
         set_cond(c->h_search, ok && accepted && c->need_search);
-        set_cond(c->h_loop,
-                 ok && (too_large || (c->steps < c->steps_target && !c->stop_hit)));
+        const int more = ok && (too_large || (c->steps < c->steps_target && !c->stop_hit));
+        set_cond(c->h_loop, more);
+        // the last iteration's removal / search are decided above; clearing
+        // the mode here spares the host a control-block write per launch
+        if (!more) c->graph_mode = 0;
     }
 }
 

@@ -263,26 +263,28 @@ int build_graph(cb_context *c) {
     return c->push();
 }
 
+// Expects hctrl to hold the device's control block (integrate_impl has just
+// read it). One asynchronous write of the control block, the graph launch
+// and one read back: the device clears graph_mode when its loop ends.
 int integrate_graph(cb_context *c, int64_t n_steps) {
     int rc = build_graph(c);
-    if (rc) return rc;
-    rc = c->pull();
     if (rc) return rc;
     Ctrl &h = *c->hctrl;
     const long long a0 = h.attempts, s0 = h.searches, d0 = h.delete_events;
     h.steps_target = h.steps + n_steps;
     h.graph_mode = 1;
-    rc = c->push();
-    if (rc) return rc;
+    // hctrl is pinned and not touched again before the synchronising read
+    CB_CUDA(cudaMemcpyAsync(c->dctrl, c->hctrl, sizeof(Ctrl), cudaMemcpyHostToDevice, c->stream));
     CB_CUDA(cudaGraphLaunch(c->gexec, c->stream));
     rc = c->pull();
     if (rc) return rc;
     c->launches += (h.attempts - a0) * kKernelsPerAttempt +
                    (h.searches - s0) * kKernelsPerSearch +
                    (h.delete_events - d0) * kKernelsPerRemove;
-    h.graph_mode = 0;
-    rc = c->push();
-    if (rc) return rc;
+    if (h.graph_mode) {  // the loop did not run to its end (a launch failure)
+        h.graph_mode = 0;
+        if ((rc = c->push())) return rc;
+    }
     if (h.status != CB_OK) return fail(h.status, status_text(h.status));
     return CB_OK;
 }
@@ -813,10 +815,9 @@ static int integrate_impl(cb_context *c, int64_t n_steps) {
 int cb_integrate(cb_context *c, int64_t n_steps, cb_report *r) {
     CB_ENTER(c);
     const int rc = integrate_impl(c, n_steps);
-    if (r) {
-        c->pull();
-        fill_report(c, r);
-    }
+    // integrate_impl leaves hctrl as read from the device after its last
+    // launch (or before, when it returned early)
+    if (r) fill_report(c, r);
     return rc;
 }
 
