@@ -521,7 +521,7 @@ def measure_batch(args, world, rank):
     import cubble_gb300 as cb
     from cubble_gb300 import workloads
     items = workloads.sweep(count=args.batch_count, seed=4 + 1000 * rank, precision=1,
-                            use_graph=1)
+                            use_graph=args.batch_graph)
     t0 = time.perf_counter()
     batch = cb.GpuFoamBatch([c for c, _ in items])
     for (cfg, st), f in zip(items, batch.foams):
@@ -712,6 +712,9 @@ def main():
     ap.add_argument("--batch-count", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=300)
     ap.add_argument("--batch-tune-steps", type=int, default=10)
+    # 0: eager batched launches (each batched kernel a separate launch, for
+    # a profiler's launch list); the measurement uses the graph
+    ap.add_argument("--batch-graph", type=int, default=1)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
