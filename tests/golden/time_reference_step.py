@@ -15,9 +15,10 @@ makes every time. Attempts repeat from the same state (no accept), timed
 with CUDA events after 3 warm-up attempts; this library's attempts are timed
 the same way (cb_profile_kernels: predict + pairs + correct, no accept).
 
-    python tests/golden/time_reference_step.py [attempts]
+    python tests/golden/time_reference_step.py [attempts] [c2|c1]
 
-prints one JSON line.
+prints one JSON line. c1 is the 2D periodic N = 10^4 foam of the CPU-runnable
+configuration, prepared the same way.
 """
 import ctypes as C
 import json
@@ -34,12 +35,13 @@ sys.path.insert(0, HERE)
 import make_golden as mg  # noqa: E402
 
 
-def main(reps):
+def main(reps, wl="c2"):
     import torch
     import cubble_gb300 as cb
     from cubble_gb300 import workloads
     cb.build()
-    cfg, st = workloads.config_c2()
+    make = workloads.config_c1 if wl == "c1" else workloads.config_c2
+    cfg, st = make()
     g = cb.GpuFoam(cfg)
     g.load_state(st)
     workloads.prepare(g)
@@ -49,7 +51,7 @@ def main(reps):
     dt = g.report()["time_step"]
     ours64 = g.profile_kernels(reps=reps)
     g.close()
-    cfg_m, _ = workloads.config_c2(precision=1)
+    cfg_m, _ = make(precision=1)
     m = cb.GpuFoam(cfg_m)
     m.load_state(s)
     m.set_pairs(pi, pj)
@@ -100,7 +102,8 @@ def main(reps):
     ref_kernels = timed(False)
     ref_step = timed(True)
     line = {
-        "what": "one step() attempt of the 3D periodic N=1e6 foam, same state and pair list",
+        "what": ("one step() attempt of the %s foam, same state and pair list"
+                 % ("2D periodic N=1e4" if wl == "c1" else "3D periodic N=1e6")),
         "bubbles": n, "pairs": int(len(pi)), "attempts_timed": reps,
         "reference_cuda_ms_per_attempt": ref_step,
         "reference_cuda_kernels_only_ms_per_attempt": ref_kernels,
@@ -117,4 +120,4 @@ def main(reps):
 
 
 if __name__ == "__main__":
-    main(int(sys.argv[1]) if len(sys.argv) > 1 else 20)
+    main(int(sys.argv[1]) if len(sys.argv) > 1 else 20, sys.argv[2] if len(sys.argv) > 2 else "c2")
