@@ -392,24 +392,6 @@ __device__ __forceinline__ double min_nonneg(double a, double b) {
     return __longlong_as_double(min(__double_as_longlong(a), __double_as_longlong(b)));
 }
 
-// Second-order variant (one Newton step, ~2^-44 relative): for square roots
-// whose result is only summed or compared (path increments, expansion), two
-// FP64 instructions fewer.
-__device__ __forceinline__ double rsqrt_hn2(double a) {
-    const double y = rsqrt_seed(a);
-    const double t = a * y;
-    const double e = fma(-t, y, 1.0);
-    return fma(0.5 * y, e, y);
-}
-__device__ __forceinline__ double sqrt_hn2(double a) {
-    return __double_as_longlong(a) > 0 ? a * rsqrt_hn2(a) : 0.0;
-}
-
-// sqrt(a) = a / sqrt(a) for a > 0, 0 for a <= 0.
-__device__ __forceinline__ double sqrt_hn(double a) {
-    return __double_as_longlong(a) > 0 ? a * rsqrt_hn(a) : 0.0;
-}
-
 // Minimum image on a periodic axis: |d| > L/2 is tested on the 32-bit words
 // of the bit patterns (non-negative doubles order like their bits; compared
 // as one 64-bit integer, the test is turned back into an FP64 compare), so

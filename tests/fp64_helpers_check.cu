@@ -1,6 +1,7 @@
 // Test harness: evaluates the FP64 helpers of the step kernels (rcp_hn,
-// rsqrt_hn, sqrt_hn, min_image) next to CUDA's IEEE division, rsqrt() and
-// sqrt() on the same inputs. Built by tests/test_gpu_math.py.
+// rsqrt_hn, and rcp_d / rsqrt_d with their float-float estimates, min_image)
+// next to CUDA's IEEE division and rsqrt() on the same inputs. Built by
+// tests/test_gpu_math.py.
 #include "../cubble_gb300/csrc/common.cuh"
 
 __global__ void k_check(const double *in, int n, double *out) {
@@ -10,8 +11,8 @@ __global__ void k_check(const double *in, int n, double *out) {
         out[8 * i + 1] = 1.0 / a;
         out[8 * i + 2] = cbg::rsqrt_hn(a);
         out[8 * i + 3] = rsqrt(a);
-        out[8 * i + 4] = cbg::sqrt_hn(a);
-        out[8 * i + 5] = sqrt(a);
+        out[8 * i + 4] = cbg::rcp_d(a);
+        out[8 * i + 5] = cbg::rsqrt_d(a);
         out[8 * i + 6] = cbg::min_image(a - 50.0, 40.0, 80.0);
         const double d = a - 50.0, t = 80.0 - fabs(d);
         out[8 * i + 7] = t * t < d * d ? t * (d < 0 ? 1.0 : -1.0) : d;

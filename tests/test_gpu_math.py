@@ -1,6 +1,6 @@
 """GPU check of the FP64 helpers the step kernels use instead of IEEE
-division / rsqrt / sqrt: they must agree with CUDA's results to a few ulp
-over the argument range of the step (radii, squared distances, areas)."""
+division and rsqrt: they must agree with CUDA's results to a few ulp over the
+argument range of the step (radii, squared distances, areas)."""
 import ctypes as C
 import os
 import subprocess
@@ -28,7 +28,7 @@ def checker():
     return lib
 
 
-def test_rcp_rsqrt_sqrt_within_a_few_ulp(checker):
+def test_rcp_rsqrt_within_a_few_ulp(checker):
     rng = np.random.default_rng(0)
     x = np.concatenate([np.logspace(-12, 12, 200001), rng.uniform(1e-3, 50.0, 200000),
                         np.array([1.0, 2.0, 4.0, 0.25, 1e-300 * 1e290])])
@@ -38,7 +38,10 @@ def test_rcp_rsqrt_sqrt_within_a_few_ulp(checker):
     eps = np.finfo(np.float64).eps
     assert rel(out[:, 0], out[:, 1]) <= 4 * eps
     assert rel(out[:, 2], out[:, 3]) <= 4 * eps
-    assert rel(out[:, 4], out[:, 5]) <= 4 * eps
+    # the helpers of the FP64 pair, predict and correct kernels (1 and 2
+    # FP64 instructions): within 2 ulp of IEEE division and rsqrt()
+    assert rel(out[:, 4], out[:, 1]) <= 2 * eps
+    assert rel(out[:, 5], out[:, 3]) <= 2 * eps
 
 
 def test_min_image_matches_reference_formula(checker):
