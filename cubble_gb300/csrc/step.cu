@@ -41,8 +41,12 @@ __device__ __forceinline__ void st_rec(float4 *R, int i, double r, double inv, d
 __device__ __forceinline__ bool ff_less(ff a, ff b) {  // normalised pairs
     return a.h < b.h || (a.h == b.h && a.l < b.l);
 }
+// Reduction of a float-float value into an FP64 row: both parts widened
+// exactly on the integer pipe and summed by one FP64 add (correctly rounded).
+// The float-float pair kernel is bound by issue slots and leaves the FP64
+// pipe mostly idle, so this costs fewer slots than the integer-pipe rounding.
 __device__ __forceinline__ void add_d(double *p, ff v) {
-    asm volatile("red.global.add.f64 [%0], %1;" ::"l"(p), "d"(ff_to_double(v)));
+    asm volatile("red.global.add.f64 [%0], %1;" ::"l"(p), "d"(ff_f2d(v.h) + ff_f2d(v.l)));
 }
 
 // ---------------------------------------------------------------- predict
