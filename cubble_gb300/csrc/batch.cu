@@ -264,6 +264,7 @@ int batch_fail_status(cb_batch *b) {
 }
 
 int batch_integrate(cb_batch *b, int64_t n_steps, cb_report *reports, double *ms) {
+    cbg::note_call();  // runs every foam's kernels
     NvtxRange nv("Batch integration");
     CB_CUDA(cudaSetDevice(b->dev));
     if (n_steps < 0) return fail(CB_ERR_INVALID_ARGUMENT, "n_steps must be >= 0");

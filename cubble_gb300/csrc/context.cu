@@ -36,6 +36,7 @@ const char *status_text(int s) {
 }
 
 void set_last_error(const std::string &msg) { g_err = msg; }
+std::atomic<unsigned long long> g_calls{0};
 }  // namespace cbg
 
 
@@ -264,8 +265,9 @@ int build_graph(cb_context *c) {
 }
 
 // Expects hctrl to hold the device's control block (integrate_impl has just
-// read it). One asynchronous write of the control block, the graph launch
-// and one read back: the device clears graph_mode when its loop ends.
+// read it, or the previous graph integration left it so). One asynchronous
+// write of the control block, the graph launch and one read back: the device
+// clears graph_mode when its loop ends.
 int integrate_graph(cb_context *c, int64_t n_steps) {
     int rc = build_graph(c);
     if (rc) return rc;
@@ -462,6 +464,7 @@ int cb_destroy(cb_context *c) {
 #define CB_ENTER(c)                                                                         \
     do {                                                                                    \
         if (!(c)) return fail(CB_ERR_INVALID_ARGUMENT, "null context");                     \
+        cbg::note_call();                                                                   \
         CB_CUDA(cudaSetDevice((c)->dev));                                                   \
     } while (0)
 
@@ -801,20 +804,28 @@ int cb_attempt(cb_context *c, cb_attempt_view *o) {
     return CB_OK;
 }
 
-static int integrate_impl(cb_context *c, int64_t n_steps) {
+// fresh: hctrl already holds the device's control block (no read needed)
+static int integrate_impl(cb_context *c, int64_t n_steps, bool fresh) {
     NvtxRange nv("Integration");
     if (!c->loaded) return fail(CB_ERR_STATE, "state not loaded");
     if (n_steps < 0) return fail(CB_ERR_INVALID_ARGUMENT, "negative step count");
-    int rc = c->pull();
-    if (rc) return rc;
+    if (!fresh) {
+        int rc = c->pull();
+        if (rc) return rc;
+    }
     if (c->hctrl->status != CB_OK) return fail(c->hctrl->status, status_text(c->hctrl->status));
     if (n_steps == 0) return CB_OK;
     return c->cfg.use_graph ? integrate_graph(c, n_steps) : integrate_eager(c, n_steps);
 }
 
 int cb_integrate(cb_context *c, int64_t n_steps, cb_report *r) {
+    // back-to-back graph integrations skip the control-block read: no call
+    // has run on any context since the last one returned
+    const bool fresh = c && c->mirror_call == cbg::g_calls.load(std::memory_order_relaxed);
     CB_ENTER(c);
-    const int rc = integrate_impl(c, n_steps);
+    c->mirror_call = ~0ull;
+    const int rc = integrate_impl(c, n_steps, fresh);
+    if (rc == CB_OK && c->cfg.use_graph) c->mirror_call = cbg::g_calls.load(std::memory_order_relaxed);
     // integrate_impl leaves hctrl as read from the device after its last
     // launch (or before, when it returned early)
     if (r) fill_report(c, r);
@@ -825,7 +836,7 @@ int cb_integrate_timed(cb_context *c, int64_t n_steps, cb_report *r, double *ms)
     CB_ENTER(c);
     CB_CUDA(cudaStreamSynchronize(c->stream));
     CB_CUDA(cudaEventRecord(c->ev0, c->stream));
-    const int rc = integrate_impl(c, n_steps);
+    const int rc = integrate_impl(c, n_steps, false);
     CB_CUDA(cudaEventRecord(c->ev1, c->stream));
     CB_CUDA(cudaEventSynchronize(c->ev1));
     float t = 0.f;
@@ -851,7 +862,7 @@ int cb_integrate_until(cb_context *c, int64_t max_steps, const cb_stop *stop, cb
     h.stop_nmin = stop->min_count;
     h.stop_rmax = stop->max_radius;
     if ((rc = c->push())) return rc;
-    rc = integrate_impl(c, max_steps);
+    rc = integrate_impl(c, max_steps, false);
     int rc2 = c->pull();
     h.stop_on = 0;
     h.stop_hit = 0;

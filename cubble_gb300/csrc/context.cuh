@@ -2,6 +2,7 @@
 // the batched foams (batch.cu). Not part of the C ABI.
 #pragma once
 
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -16,6 +17,11 @@ const char *status_text(int s);
 constexpr int kKernelsPerAttempt = 3;
 constexpr int kKernelsPerRemove = 9;
 constexpr int kKernelsPerSearch = 17;
+// Count of C-ABI calls that may touch a context, process wide: a context
+// whose host mirror was left current by a call knows, by this count, that no
+// call has run since.
+extern std::atomic<unsigned long long> g_calls;
+inline unsigned long long note_call() { return g_calls.fetch_add(1, std::memory_order_relaxed) + 1; }
 }  // namespace cbg
 
 #define CB_CUDA(x)                                                                          \
@@ -52,6 +58,9 @@ struct cb_context {
     cudaGraphExec_t gexec = nullptr;
     int graph_key = -1;
     long long graph_attempts0 = 0, graph_searches0 = 0, graph_deletes0 = 0;
+    // g_calls when a graph cb_integrate returned with hctrl equal to the
+    // device's control block and the stream idle
+    unsigned long long mirror_call = ~0ull;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
     template <typename T>

@@ -104,6 +104,7 @@ __global__ void __launch_bounds__(kBlock) k_assign(const DevConst *kp, int3 bpd,
 #define CB_ENTER(c)                                                          \
     do {                                                                     \
         if (!(c)) return fail(CB_ERR_INVALID_ARGUMENT, "null context");      \
+        cbg::note_call();                                                    \
         CB_CUDA(cudaSetDevice((c)->dev));                                    \
     } while (0)
 

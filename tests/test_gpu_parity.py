@@ -257,6 +257,34 @@ def test_graph_matches_eager(oracle_mod):
     assert b.launch_count() > 0
 
 
+@pytest.mark.parametrize("precision", [0, 2])
+def test_single_steps_with_calls_between(oracle_mod, precision):
+    """Back-to-back graph cb_integrate(1) calls reuse the host copy of the
+    control block; any other call in between makes the next one read it from
+    the device again. Here a neighbour search (it changes the pair count on
+    the device only) and an option change sit between single steps; the
+    oracle runs the same sequence: same counts and pairs, states within the
+    trajectory bar."""
+    cfg, st = make("2d", use_graph=1)
+    g, o = pair_both(oracle_mod, cfg, st, precision)
+    for f in (g, o):
+        workloads.prepare(f)
+    for phase in range(3):
+        for _ in range(4):
+            rg, ro = g.integrate(1), o.integrate(1)
+            for k in ("steps", "attempts", "searches", "count", "num_pairs"):
+                assert rg[k] == ro[k], (phase, k)
+        if phase == 0:
+            for f in (g, o):
+                f.search_neighbors()
+        else:
+            for f in (g, o):
+                f.set_options(1, 0, 0)  # path no longer incremented
+    assert g.report()["num_pairs"] == o.report()["num_pairs"]
+    sg, so = by_index(g.get_state()), by_index(o.get_state())
+    assert_rows_close(sg, so, ["x", "y", "r", "path", "error"], 1e-9, "single steps ")
+
+
 def test_pair_capacity_error(oracle_mod):
     cfg, st = make("2d", pair_capacity=100)
     g = cb.GpuFoam(cfg)
