@@ -347,6 +347,68 @@ CB_HD double ff_add_small(double y, float c) {
     return ff_mkd(hi2, lo2);
 }
 
+// Leading zeros of a 32-bit word (32 for 0).
+CB_HD int ff_clz(uint32_t x) {
+#ifdef __CUDA_ARCH__
+    return __clz((int)x);
+#else
+    return x ? __builtin_clz(x) : 32;
+#endif
+}
+
+// a - b, equal to the IEEE FP64 subtraction bit for bit, on the integer pipe
+// when it needs no rounding and the operands are alike: same sign, normal,
+// biased exponents above 64 and at most one apart, and |a| - |b| within 53
+// significant bits (Sterbenz's case b/2 <= a <= 2b always is: two nearby
+// positions, a position and its update). Then the difference of the integer
+// significands (the larger exponent's shifted left by one) is exact, and is
+// renormalised with a count of leading zeros. Everything else: the FP64
+// subtraction, as a call.
+CB_SLOW double sub_slow(double a, double b) { return a - b; }
+CB_HD double sub_exact(double a, double b) {
+    const uint32_t ah = ff_dhi(a), al = ff_dlo(a), bh = ff_dhi(b), bl = ff_dlo(b);
+    const int ea = (int)((ah >> 20) & 0x7ffu), eb = (int)((bh >> 20) & 0x7ffu);
+    const int d = ea - eb;
+    // significands with the hidden bit as (high, low) words
+    uint32_t mah = (ah & 0xfffffu) | 0x100000u, mal = al;
+    uint32_t mbh = (bh & 0xfffffu) | 0x100000u, mbl = bl;
+    if (d > 0) {
+        mah = (mah << 1) | (mal >> 31);
+        mal <<= 1;
+    } else if (d < 0) {
+        mbh = (mbh << 1) | (mbl >> 31);
+        mbl <<= 1;
+    }
+    // D = Ma - Mb over 64 bits, then |D|
+    uint32_t dl = mal - mbl;
+    uint32_t dh = mah - mbh - (mal < mbl ? 1u : 0u);
+    const bool neg = (dh & 0x80000000u) != 0;
+    if (neg) {
+        dl = 0u - dl;
+        dh = ~dh + (dl == 0u ? 1u : 0u);
+    }
+    const bool ok = ((ah ^ bh) & 0x80000000u) == 0u && ea > 64 && eb > 64 && ea < 0x7ff &&
+                    eb < 0x7ff && d >= -1 && d <= 1 && dh < 0x200000u;  // |D| < 2^53
+    if (!ok) return sub_slow(a, b);
+    if ((dh | dl) == 0u) return 0.0;  // +0, as IEEE round-to-nearest
+    const int lz = dh ? ff_clz(dh) : 32 + ff_clz(dl);  // 11 .. 63
+    const int sh = lz - 11;                            // leading bit to bit 52
+    uint32_t mh, ml;
+    if (sh >= 32) {
+        mh = dl << (sh - 32);
+        ml = 0u;
+    } else if (sh > 0) {
+        mh = (dh << sh) | (dl >> (32 - sh));
+        ml = dl << sh;
+    } else {
+        mh = dh;
+        ml = dl;
+    }
+    const uint32_t e = (uint32_t)((ea < eb ? ea : eb) - sh);  // > 11
+    const uint32_t sign = (ah & 0x80000000u) ^ (neg ? 0x80000000u : 0u);
+    return ff_mkd(sign | (e << 20) | (mh & 0xfffffu), ml);
+}
+
 // true when a > 0 and float-float holds a, its root and reciprocal root
 CB_HD bool ff_in_range(double a) {
     const int eb = (int)((ff_dhi(a) >> 20) & 0xfffu);  // sign bit included: a > 0 only

@@ -276,13 +276,14 @@ __device__ __forceinline__ void k_pairs_body(const Bufs &b, const int vb, const 
             const double4_32a a = ld4(b.pred, i), q = ld4(b.pred, j);
             r1 = DIM == 3 ? a.w : a.z;
             r2 = DIM == 3 ? q.w : q.z;
-            // wrappedDifference, src/kernels.cu:1094-1114
-            dx = a.x - q.x;
-            dy = a.y - q.y;
+            // wrappedDifference, src/kernels.cu:1094-1114 (the FP64
+            // differences, exact, mostly on the integer pipe)
+            dx = sub_exact(a.x, q.x);
+            dy = sub_exact(a.y, q.y);
             if (px) dx = min_image(dx, hx, Lx);
             if (py) dy = min_image(dy, hy, Ly);
             if (DIM == 3) {
-                dz = a.z - q.z;
+                dz = sub_exact(a.z, q.z);
                 if (pz) dz = min_image(dz, hz, Lz);
             }
             // overlap test (r1 + r2)^2 >= m: in FP32 on the exact differences

@@ -35,7 +35,8 @@ int main() {
     Max split{"split"}, back{"to_double"}, back_ulp{"to_double_ulps"}, add{"add"},
         addc{"add_cancel_abs"}, mul{"mul"}, sqr{"sqr"}, rcp{"rcp"}, rsq{"rsqrt"},
         sqt{"sqrt"}, pair{"pair_velocity"}, chord{"chord_area_abs"}, rsqd{"rsqrt_d_ulps"},
-        rcpd{"rcp_d_ulps"}, sqd{"sqrt_ffd"}, small{"add_small_ulps"};
+        rcpd{"rcp_d_ulps"}, sqd{"sqrt_ffd"}, small{"add_small_ulps"},
+        subx{"sub_exact_mismatches"};
     const int N = 400000;
     for (int it = 0; it < N; it++) {
         // split: top 24 bits exact, the rest to 2^-47
@@ -86,6 +87,20 @@ int main() {
             const ld zq = (ld)y + (ld)cc;
             small.add((z > zq ? z - zq : zq - z) / (ld)std::ldexp(1.0, std::ilogb(z) - 52));
         }
+        // exact subtraction: bit-identical to the FP64 one on nearby values
+        // (both signs, across binade edges, equal), far apart, zeros and
+        // values of opposite sign
+        {
+            double p = sgn() * logu(-40, 40);
+            if (it % 3 == 0) p = sgn() * std::ldexp(1.0, (int)(U(rng) * 60) - 30);
+            double q = p + sgn() * std::fabs(p) * logu(-55, 2);
+            if (it % 11 == 0) q = p;
+            if (it % 13 == 0) q = -q;
+            if (it % 17 == 0) q = 0.0;
+            if (it % 19 == 0) p = std::ldexp(p, -1000);
+            const double want = p - q, got = cbg::sub_exact(p, q);
+            if (std::memcmp(&want, &got, 8) != 0) subx.add(subx.v + 1);
+        }
         // the pair velocity factor f0 (1/|d| - 1/(r1 + r2)) and the chord
         // area r2^2 - w^2 / 4, w = (r2^2 - r1^2 + m) / |d|, on overlapping
         // pairs of radii ~ 1 (|d| < r1 + r2)
@@ -116,7 +131,7 @@ int main() {
         chord.add((val(oa) > oaL ? val(oa) - oaL : oaL - val(oa)) / scale);
     }
     for (Max *m : {&split, &back, &back_ulp, &add, &addc, &mul, &sqr, &rcp, &rsq, &sqt, &pair,
-                   &chord, &rsqd, &rcpd, &sqd, &small})
+                   &chord, &rsqd, &rcpd, &sqd, &small, &subx})
         std::printf("%s %.6Le\n", m->name, m->v);
     return 0;
 }

@@ -55,3 +55,27 @@ extern "C" int ff_check(const double *host_in, int n, double *host_out) {
     cudaFree(dout);
     return e == cudaSuccess ? 0 : 2;
 }
+
+// The exact subtraction of the FP64 pair kernel (ff.cuh sub_exact) next to
+// the FP64 subtraction on the same operand pairs.
+__global__ void k_sub_check(const double *a, const double *b, int n, double *out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        out[2 * i + 0] = cbg::sub_exact(a[i], b[i]);
+        out[2 * i + 1] = __dsub_rn(a[i], b[i]);
+    }
+}
+
+extern "C" int sub_check(const double *ha, const double *hb, int n, double *host_out) {
+    double *da = nullptr, *db = nullptr, *dout = nullptr;
+    if (cudaMalloc(&da, n * sizeof(double)) != cudaSuccess) return 1;
+    if (cudaMalloc(&db, n * sizeof(double)) != cudaSuccess) return 1;
+    if (cudaMalloc(&dout, 2 * n * sizeof(double)) != cudaSuccess) return 1;
+    cudaMemcpy(da, ha, n * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(db, hb, n * sizeof(double), cudaMemcpyHostToDevice);
+    k_sub_check<<<256, 256>>>(da, db, n, dout);
+    cudaError_t e = cudaMemcpy(host_out, dout, 2 * n * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaFree(da);
+    cudaFree(db);
+    cudaFree(dout);
+    return e == cudaSuccess ? 0 : 2;
+}

@@ -43,6 +43,12 @@ def test_operations(errors, op):
     assert errors[op] <= 2.0 ** -45, (op, errors[op])
 
 
+def test_exact_subtraction_bit_identical(errors):
+    """sub_exact (the FP64 pair kernel's position differences on the integer
+    pipe) equals the FP64 subtraction bit for bit."""
+    assert errors["sub_exact_mismatches"] == 0
+
+
 def test_fp64_results_with_few_fp64_instructions(errors):
     """1/sqrt and 1/x of the FP64 kernels (float-float estimate, one FP64
     residual, the correction added on the integer pipe): within 1 ulp; the

@@ -67,3 +67,27 @@ def test_float_float_helpers_on_device(checker):
     assert rel(out[:, 1], 1 / L) <= 2.0 ** -45
     assert rel(out[:, 2], 1 / np.sqrt(L)) <= 2.0 ** -45
     assert rel(out[:, 3], np.sqrt(L)) <= 2.0 ** -45
+
+
+def test_exact_subtraction_on_device(checker):
+    """The FP64 pair kernel's position differences (sub_exact: integer
+    significands when the difference needs no rounding, the FP64 subtraction
+    otherwise) are bit-identical to the FP64 subtraction: nearby values of
+    both signs, across binade edges, equal, far apart, of opposite sign,
+    zeros and subnormals."""
+    checker.sub_check.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+    rng = np.random.default_rng(2)
+    n = 400000
+    a = rng.choice([-1.0, 1.0], n) * np.exp2(rng.uniform(-40, 40, n))
+    a[::3] = np.sign(a[::3]) * np.exp2(np.round(rng.uniform(-30, 30, len(a[::3]))))
+    b = a + rng.choice([-1.0, 1.0], n) * np.abs(a) * np.exp2(rng.uniform(-55, 2, n))
+    b[::11] = a[::11]
+    b[::13] = -b[::13]
+    b[::17] = 0.0
+    a[::19] = a[::19] * 2.0 ** -1060
+    box = rng.uniform(0.0, 175.0, n // 4)  # positions of nearby bubbles in a box
+    a = np.concatenate([a, box])
+    b = np.concatenate([b, box + rng.normal(0.0, 2.0, len(box))])
+    out = np.zeros((len(a), 2))
+    assert checker.sub_check(a.ctypes.data, b.ctypes.data, len(a), out.ctypes.data) == 0
+    assert np.array_equal(out[:, 0].view(np.int64), out[:, 1].view(np.int64))
