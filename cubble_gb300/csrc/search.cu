@@ -522,16 +522,24 @@ __device__ __forceinline__ void k_pair_rows_body(const Bufs &b, const int vb, co
             }
             nb[p] = v;
         }
+        // the candidates of all listed cells as one flat sequence: a lane
+        // moves to its next cell inside the loop, so the warp runs for its
+        // longest lane's candidate count, not for the sum over cells of the
+        // longest lane's count in each
         int cnt = 0;
-        for (int t = 0; t < nq; t++) {
-            const int qc = nb[t];
-            const int ce = b.cellStart[qc + 1];
-            for (int j = max(b.cellStart[qc], i + 1); j < ce; j++) {
-                if (pair_take<DIM>(k, pi, b.pos32[j], i, j, X, Y, Z, R)) {
-                    if (cnt < M) b.stash[(size_t)i * M + cnt] = j;
-                    cnt++;
-                }
+        int t = -1, j = 0, je = 0;
+        while (true) {
+            while (j >= je && ++t < nq) {
+                const int qc = nb[t];
+                j = max(b.cellStart[qc], i + 1);
+                je = b.cellStart[qc + 1];
             }
+            if (t >= nq) break;
+            if (pair_take<DIM>(k, pi, b.pos32[j], i, j, X, Y, Z, R)) {
+                if (cnt < M) b.stash[(size_t)i * M + cnt] = j;
+                cnt++;
+            }
+            j++;
         }
         NN[i] = cnt;
         b.rowCount[i] = cnt;
