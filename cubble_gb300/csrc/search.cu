@@ -323,10 +323,29 @@ static __device__ __noinline__ bool pair_take_exact(const DevConst &k, int i, in
                                         DIM == 3 ? Z[j] : 0.0);
     return sq < __dmul_rn(maxd, maxd);
 }
+// pair_class on a difference that needs no minimum image: `ps` is the
+// bubble's position already moved by the periodic image shift of the
+// candidate's cell.
 template <int DIM>
-__device__ __forceinline__ bool pair_take(const DevConst &k, const float4 &pi, const float4 &pj,
-                                          int i, int j, const double *X, const double *Y,
-                                          const double *Z, const double *R) {
+__device__ __forceinline__ int pair_class_direct(const DevConst &k, const float4 &ps,
+                                                 const float4 &pj) {
+    const float dx = ps.x - pj.x, dy = ps.y - pj.y;
+    float d2 = fmaf(dx, dx, dy * dy);
+    if (DIM == 3) {
+        const float dz = ps.z - pj.z;
+        d2 = fmaf(dz, dz, d2);
+    }
+    const float cut = ps.w + pj.w + k.skin_f;
+    const float band = k.pre_margin;
+    const float hi = cut + band, lo = fmaxf(cut - band, 0.f);
+    if (d2 >= hi * hi) return 0;
+    if (d2 < lo * lo) return 1;
+    return 2;
+}
+// The FP32 part of the test: 0 not a partner, 1 a partner, 2 within the
+// guard band (the exact test decides).
+template <int DIM>
+__device__ __forceinline__ int pair_class(const DevConst &k, const float4 &pi, const float4 &pj) {
     const bool per[3] = {!k.wall[0], !k.wall[1], !k.wall[2]};
     float dx = fabsf(pi.x - pj.x), dy = fabsf(pi.y - pj.y);
     float dz = DIM == 3 ? fabsf(pi.z - pj.z) : 0.f;
@@ -338,9 +357,16 @@ __device__ __forceinline__ bool pair_take(const DevConst &k, const float4 &pi, c
     const float cut = pi.w + pj.w + k.skin_f;
     const float band = k.pre_margin;
     const float hi = cut + band, lo = fmaxf(cut - band, 0.f);
-    if (d2 >= hi * hi) return false;
-    if (d2 < lo * lo) return true;
-    return pair_take_exact<DIM>(k, i, j, X, Y, Z, R);
+    if (d2 >= hi * hi) return 0;
+    if (d2 < lo * lo) return 1;
+    return 2;
+}
+template <int DIM>
+__device__ __forceinline__ bool pair_take(const DevConst &k, const float4 &pi, const float4 &pj,
+                                          int i, int j, const double *X, const double *Y,
+                                          const double *Z, const double *R) {
+    const int cls = pair_class<DIM>(k, pi, pj);
+    return cls == 1 || (cls == 2 && pair_take_exact<DIM>(k, i, j, X, Y, Z, R));
 }
 
 // Pair rows of one cell per warp: lanes are the cell's bubbles (32 at a
@@ -463,6 +489,16 @@ __device__ __forceinline__ void k_pair_rows_body(const Bufs &b, const int vb, co
 #pragma unroll
     for (int a = 0; a < 3; a++) cw[a] = k.iv32[a] / (float)cd[a];
     const float reach0 = c->search_maxr + k.skin_f + k.pre_margin + 1e-3f;
+    // with at least four cells on every periodic axis a listed cell's
+    // candidates lie within half a box of the bubble's image for that cell:
+    // the bubble is moved by the cell's image shift once, and candidates are
+    // tested on plain differences (no minimum image per candidate). 3D only:
+    // 2D cells hold ~3 bubbles, and the shift per cell then costs more than
+    // the minimum image per candidate (measured on GB300: 3D N = 10^6 search
+    // 0.966 -> 0.926 ms, 2D 1.042 -> 1.080 ms)
+    bool direct = DIM == 3;
+#pragma unroll
+    for (int a = 0; a < DIM; a++) direct &= k.wall[a] || cd[a] >= 4;
     bool over = false;
     for (int i = vb * blockDim.x + threadIdx.x; i < n; i += vg * blockDim.x) {
         const int cell = b.cellSorted[i];
@@ -479,6 +515,7 @@ __device__ __forceinline__ void k_pair_rows_body(const Bufs &b, const int vb, co
             hi[a] = fmaxf((float)(kk[a] + 1) * cw[a] - pr[a], 0.f);
         }
         int nb[NO];
+        int ns[NO];  // image shift per listed cell: 2 bits per axis, 1 = +L, 2 = -L
         int nq = 0;
 #pragma unroll
         for (int t = 0; t < NO; t++) {
@@ -486,6 +523,7 @@ __device__ __forceinline__ void k_pair_rows_body(const Bufs &b, const int vb, co
             const int off[3] = {o % 3 - 1, (o / 3) % 3 - 1, o / 9 - 1};
             // neighbour cell index (getNeighborCellIndex, src/kernels.cu:1157-1189)
             int q[3];
+            int sh = 0;
             bool ok = true;
 #pragma unroll
             for (int a = 0; a < 3; a++) {
@@ -496,6 +534,7 @@ __device__ __forceinline__ void k_pair_rows_body(const Bufs &b, const int vb, co
                 } else if (!k.wall[a]) {
                     ok &= !(d == 1 && off[a] != 0) && !(d == 2 && off[a] == -1);
                     q[a] = kk[a] + off[a];
+                    sh |= (q[a] < 0 ? 1 : (q[a] >= d ? 2 : 0)) << (2 * a);
                     q[a] = q[a] < 0 ? q[a] + d : (q[a] >= d ? q[a] - d : q[a]);
                 } else {
                     q[a] = kk[a] + off[a];
@@ -518,9 +557,11 @@ __device__ __forceinline__ void k_pair_rows_body(const Bufs &b, const int vb, co
             int p = nq++;  // insertion into the ascending list
             while (p > 0 && nb[p - 1] > v) {
                 nb[p] = nb[p - 1];
+                ns[p] = ns[p - 1];
                 p--;
             }
             nb[p] = v;
+            ns[p] = sh;
         }
         // the candidates of all listed cells as one flat sequence: a lane
         // moves to its next cell inside the loop, so the warp runs for its
@@ -528,14 +569,23 @@ __device__ __forceinline__ void k_pair_rows_body(const Bufs &b, const int vb, co
         // longest lane's count in each
         int cnt = 0;
         int t = -1, j = 0, je = 0;
+        float4 ps = pi;
         while (true) {
             while (j >= je && ++t < nq) {
                 const int qc = nb[t];
                 j = max(b.cellStart[qc], i + 1);
                 je = b.cellStart[qc + 1];
+                const int sh = ns[t];
+                const float s[3] = {
+                    (sh & 1) ? k.iv32[0] : ((sh & 2) ? -k.iv32[0] : 0.f),
+                    (sh & 4) ? k.iv32[1] : ((sh & 8) ? -k.iv32[1] : 0.f),
+                    (sh & 16) ? k.iv32[2] : ((sh & 32) ? -k.iv32[2] : 0.f)};
+                ps = make_float4(pi.x + s[0], pi.y + s[1], pi.z + s[2], pi.w);
             }
             if (t >= nq) break;
-            if (pair_take<DIM>(k, pi, b.pos32[j], i, j, X, Y, Z, R)) {
+            const float4 pj = b.pos32[j];
+            const int cls = direct ? pair_class_direct<DIM>(k, ps, pj) : pair_class<DIM>(k, pi, pj);
+            if (cls == 1 || (cls == 2 && pair_take_exact<DIM>(k, i, j, X, Y, Z, R))) {
                 if (cnt < M) b.stash[(size_t)i * M + cnt] = j;
                 cnt++;
             }
