@@ -64,6 +64,7 @@ __device__ __forceinline__ void k_predict_body(const Bufs &b, const int vb, cons
     const double *O0 = drow(b, c, RVO0), *O1 = drow(b, c, RVO1), *O2 = drow(b, c, RVO2),
                  *O3 = drow(b, c, RVO3);
     double sA = 0.0, sAr = 0.0;
+    int na = 0;
     for (int i = vb * blockDim.x + threadIdx.x; i < n; i += vg * blockDim.x) {
         // p + 0.5 ts (3 v - vo), src/kernels.cu:48-50
         const double xp = fma(h, fma(3.0, V0[i], -O0[i]), X[i]);
@@ -87,14 +88,21 @@ __device__ __forceinline__ void k_predict_body(const Bufs &b, const int vb, cons
             p.w = inv;
         }
         reinterpret_cast<double4_32a *>(b.pred)[i] = p;
-        if (gas) {  // area and area per radius, src/kernels.cu:103-112
-            const double apr = DIM == 3 ? (4.0 * kPi) * rp : 2.0 * kPi;
-            sA = fma(apr, rp, sA);
-            sAr += apr;
+        if (gas) {  // area and area per radius, src/kernels.cu:103-112, with
+                    // the constant factor (4 pi, 2 pi) applied to the block sums
+            if (DIM == 3) {
+                sA += rsq;
+                sAr += rp;
+            } else {
+                sA += rp;
+                na++;
+            }
         }
     }
-    const double tA = block_reduce(sA, OpSum(), smem);
-    const double tAr = block_reduce(sAr, OpSum(), smem);
+    if (DIM == 2) sAr = (double)na;
+    constexpr double kArea = DIM == 3 ? 4.0 * kPi : 2.0 * kPi;
+    const double tA = kArea * block_reduce(sA, OpSum(), smem);
+    const double tAr = kArea * block_reduce(sAr, OpSum(), smem);
     if (threadIdx.x == 0) {
         b.part[0 * vg + vb] = tA;
         b.part[1 * vg + vb] = tAr;
