@@ -710,7 +710,7 @@ def main():
     ap.add_argument("--chunk-steps", type=int, default=2000)
     ap.add_argument("--max-run-steps", type=int, default=200000)
     ap.add_argument("--batch-count", type=int, default=256)
-    ap.add_argument("--batch-steps", type=int, default=300)
+    ap.add_argument("--batch-steps", type=int, default=5000)  # the sweep runs 5,000 steps per foam
     ap.add_argument("--batch-tune-steps", type=int, default=10)
     # 0: eager batched launches (each batched kernel a separate launch, for
     # a profiler's launch list); the measurement uses the graph
