@@ -285,6 +285,29 @@ def test_single_steps_with_calls_between(oracle_mod, precision):
     assert_rows_close(sg, so, ["x", "y", "r", "path", "error"], 1e-9, "single steps ")
 
 
+def test_two_foams_alternating_single_steps():
+    """Single graph steps alternating between two contexts: each call finds
+    the other context's call in between and reads its control block again,
+    and each foam follows the trajectory it has when run alone."""
+    cfg, st = make("2d", use_graph=1)
+    a, b, solo = cb.GpuFoam(cfg), cb.GpuFoam(cfg), cb.GpuFoam(cfg)
+    for f in (a, b, solo):
+        f.load_state(st)
+        workloads.prepare(f)
+    for _ in range(12):
+        a.integrate(1)
+        b.integrate(1)
+        solo.integrate(1)
+    ra, rb, rs = a.report(), b.report(), solo.report()
+    for k in ("steps", "attempts", "searches", "count", "num_pairs"):
+        assert ra[k] == rs[k] and rb[k] == rs[k], k
+    ss = by_index(solo.get_state())
+    for f in (a, b):
+        assert_rows_close(by_index(f.get_state()), ss, ["x", "y", "r"], 1e-10, "alternating ")
+    for f in (a, b, solo):
+        f.close()
+
+
 def test_pair_capacity_error(oracle_mod):
     cfg, st = make("2d", pair_capacity=100)
     g = cb.GpuFoam(cfg)
