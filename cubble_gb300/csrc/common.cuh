@@ -613,11 +613,22 @@ __device__ __forceinline__ int batch_item(const BatchWork *wk, int item, int &vb
 // on a fixed grid (no block waits for another).
 // TPL is the parenthesised template header ("(template <int DIM>)" or "()"),
 // ARGS the parenthesised template arguments ("(<DIM>)" or "()").
+// Programmatic dependent launch: the kernels below are launched so that they
+// may begin while the previous kernel on the stream drains (launch_pdl). The
+// first thing each does is wait for that kernel's completion and memory
+// (griddepcontrol.wait); it then lets its own successor be scheduled.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 #define CB_KERNEL_PAIR(TPL, NAME, ARGS, BOUNDS)                                  \
     CB_ID TPL __global__ void BOUNDS NAME(Bufs b) {                                \
+        pdl_enter();                                                               \
         NAME##_body CB_ID ARGS(b, blockIdx.x, gridDim.x);                          \
     }                                                                              \
     CB_ID TPL __global__ void BOUNDS NAME##_batch(const Bufs *bb, const BatchWork *wk) { \
+        pdl_enter();                                                               \
         const int total = wk->total;                                               \
         for (int item = blockIdx.x; item < total; item += gridDim.x) {             \
             int vb, vg;                                                            \
@@ -627,13 +638,30 @@ __device__ __forceinline__ int batch_item(const BatchWork *wk, int item, int &vb
         }                                                                          \
     }
 
+// Launch of a CB_KERNEL_PAIR kernel with programmatic stream serialisation
+// (a failure is left for the caller's cudaGetLastError, as for <<<>>>).
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*kernel)(KArgs...), int grid, cudaStream_t stream, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kBlock);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // Launches NAME<ARGS> in its single or batched form per the Launch `l`.
 #define CB_LAUNCH(l, NAME, ARGS, GRID, b)                                             \
     do {                                                                             \
         if ((l).batch)                                                               \
-            NAME##_batch CB_ID ARGS<<<(l).gmax, kBlock, 0, (l).stream>>>((l).batch, (l).work); \
+            launch_pdl(NAME##_batch CB_ID ARGS, (l).gmax, (l).stream, (l).batch, (l).work); \
         else                                                                         \
-            NAME CB_ID ARGS<<<(GRID), kBlock, 0, (l).stream>>>(b);                   \
+            launch_pdl(NAME CB_ID ARGS, (GRID), (l).stream, (b));                    \
         *(l).launches += 1;                                                          \
     } while (0)
 
