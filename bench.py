@@ -672,6 +672,7 @@ def run_gb300(args, world, rank, local):
                    "graph": bool(args.graph), "parallelism": "replicas" if world > 1 else "single foam",
                    "l2": "working set larger than L2 (state + pairs > 129 MB)",
                    "attempts": attempts, "searches": searches,
+                   "steps_per_search": (args.steps / searches) if searches else None,
                    "pairs_per_bubble": main["np_per_n"], "bubbles_end": r1["count"],
                    "deleted": r1["deleted"] - r0["deleted"], "dt_end": r1["time_step"]},
         "roofline": main["roofline"], "cpu_baseline": base, "e2e": e2e,
