@@ -14,7 +14,6 @@
 // (src/kernels.cu:941-957, src/simulator.cu:39-58): per pair
 // e = r_i + r_j - |d| (minimum image), e^2 added to both bubbles when e > 0,
 // then the per-bubble energies are summed.
-#include <mutex>
 #include <string>
 
 #include "common.cuh"
@@ -29,10 +28,12 @@ using namespace cbg;
 
 constexpr int kMaxBubbles = 1 << 18;  // 262,144 bubbles
 constexpr int kBlocks = 512;          // reduction blocks (fixed)
-constexpr int kMaxDevices = 64;
 // [0, kMaxBubbles): per-bubble energies; [kMaxBubbles, +kBlocks): block
-// partials; the last word holds the last-block counter.
-constexpr int kScratchWords = kMaxBubbles + kBlocks + 1;
+// partials; then the last-block counter and the count of rejected pairs
+// (pairs with an index outside [0, count)), one word each.
+constexpr int kDoneWord = kMaxBubbles + kBlocks;
+constexpr int kBadWord = kDoneWord + 1;
+constexpr int kScratchWords = kBadWord + 1;
 
 static __device__ __align__(256) double g_scratch[kScratchWords];
 
@@ -45,22 +46,32 @@ struct Box {
 __global__ void __launch_bounds__(kBlock) k_na_clear(double *s, int n) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         s[i] = 0.0;
-    if (blockIdx.x == 0 && threadIdx.x == 0)
-        *reinterpret_cast<unsigned int *>(s + kMaxBubbles + kBlocks) = 0u;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *reinterpret_cast<unsigned int *>(s + kDoneWord) = 0u;
+        *reinterpret_cast<unsigned int *>(s + kBadWord) = 0u;
+    }
 }
 
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_na_pairs(Box box, const double *X, const double *Y,
                                                      const double *Z, const double *R,
                                                      const int *PI, const int *PJ, int np,
-                                                     double *s) {
+                                                     int n, double *s) {
     DevConst k{};
     for (int a = 0; a < 3; a++) {
         k.wall[a] = box.wall[a];
         k.iv[a] = box.iv[a];
     }
+    unsigned int bad = 0u;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
         const int i = PI[p], j = PJ[p];
+        // the indices come from the caller: one outside [0, n) would read
+        // past the caller's rows and add into scratch words that are not
+        // per-bubble energies, so it is skipped and counted instead
+        if ((unsigned)i >= (unsigned)n || (unsigned)j >= (unsigned)n) {
+            bad++;
+            continue;
+        }
         double dx, dy, dz;
         wrapped_diff<DIM>(k, X[i], Y[i], DIM == 3 ? Z[i] : 0.0, X[j], Y[j],
                           DIM == 3 ? Z[j] : 0.0, dx, dy, dz);
@@ -73,6 +84,7 @@ __global__ void __launch_bounds__(kBlock) k_na_pairs(Box box, const double *X, c
             atomicAdd(s + j, e);
         }
     }
+    if (bad) atomicAdd(reinterpret_cast<unsigned int *>(s + kBadWord), bad);
 }
 
 __global__ void __launch_bounds__(kBlock) k_na_sum(double *s, int n, double *out) {
@@ -85,45 +97,30 @@ __global__ void __launch_bounds__(kBlock) k_na_sum(double *s, int n, double *out
     const double t = block_reduce(v, OpSum(), smem);
     double *part = s + kMaxBubbles;
     if (threadIdx.x == 0) part[blockIdx.x] = t;
-    unsigned int *done = reinterpret_cast<unsigned int *>(s + kMaxBubbles + kBlocks);
+    unsigned int *done = reinterpret_cast<unsigned int *>(s + kDoneWord);
     if (last_block(done, gridDim.x)) {
         const double f = fold_partials(part, gridDim.x, false, smem);
         if (threadIdx.x == 0) {
-            *out = f;
+            const unsigned int bad = *reinterpret_cast<volatile unsigned int *>(s + kBadWord);
+            *out = bad ? __longlong_as_double(0x7ff8000000000000LL) : f;  // NaN: bad pairs
             *done = 0u;
         }
     }
 }
 
-std::mutex g_mu;
-double *g_addr[kMaxDevices] = {};
-
-// Per-device set-up: the device address of g_scratch, looked up once with
-// that device current. Host code must not use &g_scratch itself: on the host
-// it names a stand-in, not device memory.
+// The device address of g_scratch for the current device and context, looked
+// up on every call: after the module is loaded this is a host-side lookup,
+// and it stays right when the caller has reset the device or switched to
+// another context since the last call. Host code must not use &g_scratch
+// itself: on the host it names a stand-in, not device memory.
 int scratch_for_current_device(double **out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) {
-        set_last_error(std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+    if (e != cudaSuccess || !p) {
+        set_last_error(std::string("cudaGetSymbolAddress(g_scratch): ") + cudaGetErrorString(e));
         return CB_ERR_CUDA;
     }
-    if (dev < 0 || dev >= kMaxDevices) {
-        set_last_error("device ordinal out of range for the static scratch table");
-        return CB_ERR_INVALID_ARGUMENT;
-    }
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_addr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_scratch);
-        if (e != cudaSuccess || !p) {
-            set_last_error(std::string("cudaGetSymbolAddress(g_scratch): ") +
-                           cudaGetErrorString(e));
-            return CB_ERR_CUDA;
-        }
-        g_addr[dev] = static_cast<double *>(p);
-    }
-    *out = g_addr[dev];
+    *out = static_cast<double *>(p);
     return CB_OK;
 }
 
@@ -168,9 +165,11 @@ extern "C" int cb_energy_noalloc(const cb_config *cfg, const double *x, const do
     const int grid = kBlocks;
     k_na_clear<<<grid, kBlock, 0, st>>>(s, count);
     if (box.dim == 3)
-        k_na_pairs<3><<<grid, kBlock, 0, st>>>(box, x, y, z, r, pair_i, pair_j, num_pairs, s);
+        k_na_pairs<3><<<grid, kBlock, 0, st>>>(box, x, y, z, r, pair_i, pair_j, num_pairs,
+                                               count, s);
     else
-        k_na_pairs<2><<<grid, kBlock, 0, st>>>(box, x, y, z, r, pair_i, pair_j, num_pairs, s);
+        k_na_pairs<2><<<grid, kBlock, 0, st>>>(box, x, y, z, r, pair_i, pair_j, num_pairs,
+                                               count, s);
     k_na_sum<<<grid, kBlock, 0, st>>>(s, count, energy_out);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
