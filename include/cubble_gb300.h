@@ -279,6 +279,12 @@ CB_API int cb_total_volume(cb_context *ctx, double *volume);
  * measured with CUDA events on the context's stream. */
 CB_API int cb_profile_kernels(cb_context *ctx, int32_t reps, double ms[3]);
 
+/* Measurement: `reps` back-to-back searchNeighbors() (src/simulator.cu:60-178)
+ * of the current state after one untimed search; *ms = mean device time of
+ * one search (CUDA events on the context's stream). The state is left
+ * searched; the report's search counter does not count these. */
+CB_API int cb_profile_search(cb_context *ctx, int32_t reps, double *ms);
+
 /* Number of kernels this library launched on the context so far (graph
  * kernel nodes are counted per execution). */
 CB_API int cb_launch_count(cb_context *ctx, int64_t *count);
@@ -337,11 +343,16 @@ CB_API int cb_batch_launch_count(cb_batch *batch, int64_t *count);
  * enqueued there and the call returns without waiting.
  *
  * count > 262,144 is rejected with CB_ERR_CAPACITY before any GPU work.
- * The first call on a device looks up the device address of the static
- * array with that device current; make that first call before any stream
- * capture. Every call reuses the same array and clears what must start at
- * zero, so calls that overlap on the GPU (different streams, or several
- * host threads) race with each other: serialise them. */
+ * The pair indices are the caller's: a pair with i or j outside [0, count)
+ * is skipped without reading or writing anything for it, and the call's
+ * result is then NaN (the call stays asynchronous; check the value).
+ * Every call looks up the device address of the static array for the
+ * current device and context (a host-side lookup once the library's module
+ * is loaded, so it stays right after a cudaDeviceReset or a context switch);
+ * the first call on a device loads the module, so make that first call
+ * before any stream capture. Every call reuses the same array and clears
+ * what must start at zero, so calls that overlap on the GPU (different
+ * streams, or several host threads) race with each other: serialise them. */
 CB_API int cb_energy_noalloc(const cb_config *cfg, const double *x, const double *y,
                              const double *z, const double *r, const int32_t *pair_i,
                              const int32_t *pair_j, int32_t count, int32_t num_pairs,
