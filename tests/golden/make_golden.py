@@ -1,10 +1,12 @@
 """Generates the golden vectors of tests/golden/ by running the REFERENCE's own
 device code (KJLankinen/cubble src/kernels.cu, compiled unmodified by
-oracle/ref/build_ref.py into oracle/_ref/kernels_ref.cubin) on a GB300.
+oracle/ref/build_ref.py into oracle/_ref/kernels_ref.cubin) on a GB300,
+through the driver-API harness of oracle/ref/harness.py.
 
 It restates only the host glue of src/simulator.cu that the kernels need
 (launch shapes, the CUB scans as host prefix sums, the pointer rotations) and
-records, for small seeded foams:
+records, for seeded foams (2D, 3D, a wall in x, a wall in z, box flow in 2D
+and 3D, and the 2D N = 10^4 configuration):
 
   search   wrapOverPeriodicBoundaries -> cellByPosition -> scan ->
            indexByCell -> reorganizeByIndex -> neighborSearch
@@ -23,8 +25,9 @@ With --init it writes init_2d.npz / init_3d.npz instead: init()'s
 assignDataToBubbles on seeded draws and transformPositions both ways.
 
 Run on the GPU machine (torch provides the device buffers, ctypes the driver API):
-    python tests/golden/make_golden.py [out_dir]
-The .npz files it writes are committed under tests/golden/.
+    python tests/golden/make_golden.py [--init] [--only=NAME,...] OUT_DIR
+(OUT_DIR is required; --only records just the named cases). The .npz files
+it writes are committed under tests/golden/.
 """
 import ctypes as C
 import math
@@ -37,197 +40,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-CUBIN = os.path.join(ROOT, "oracle", "_ref", "kernels_ref.cubin")
-BLOCK, GRID = 384, 5120  # src/data_definitions.h:28-29
-
-DROWS = ["x", "y", "z", "r", "xp", "yp", "zp", "rp", "dxdt", "dydt", "dzdt", "drdt",
-         "dxdtp", "dydtp", "dzdtp", "drdtp", "dxdto", "dydto", "dzdto", "drdto",
-         "path", "pathNew", "error", "flowVx", "flowVy", "flowVz",
-         "savedX", "savedY", "savedZ", "savedR"]
-IROWS = ["wrapCountX", "wrapCountY", "wrapCountZ", "index", "numNeighbors"]
-
-
-class Bubbles(C.Structure):  # src/data_definitions.h:41-153
-    _fields_ = ([(n, C.c_void_p) for n in DROWS] + [(n, C.c_void_p) for n in IROWS]
-                + [("count", C.c_int32), ("stride", C.c_uint64),
-                   ("numDP", C.c_uint64), ("numIP", C.c_uint64)])
-
-
-class Pairs(C.Structure):  # src/data_definitions.h:157-178
-    _fields_ = [("i", C.c_void_p), ("j", C.c_void_p), ("count", C.c_int32),
-                ("stride", C.c_uint64)]
-
-
-class DVec(C.Structure):
-    _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double)]
-
-
-class IVec(C.Structure):
-    _fields_ = [("x", C.c_int32), ("y", C.c_int32), ("z", C.c_int32)]
-
-
-class Constants(C.Structure):  # src/data_definitions.h:183-225
-    _fields_ = [("lbb", DVec), ("tfr", DVec), ("interval", DVec), ("flowLbb", DVec),
-                ("flowTfr", DVec), ("flowVel", DVec),
-                ("averageSurfaceAreaIn", C.c_double), ("minRad", C.c_double),
-                ("fZeroPerMuZero", C.c_double), ("kParameter", C.c_double),
-                ("kappa", C.c_double), ("wallDragStrength", C.c_double),
-                ("skinRadius", C.c_double), ("bubbleVolumeMultiplier", C.c_double),
-                ("dimensionality", C.c_int32), ("xWall", C.c_bool), ("yWall", C.c_bool),
-                ("zWall", C.c_bool)]
-
-
-class Driver:
-    def __init__(self, cubin):
-        import torch
-        self.torch = torch
-        torch.zeros(1, device="cuda")  # primary context current on this thread
-        self.cu = C.CDLL("libcuda.so.1")
-        self.mod = C.c_void_p()
-        self._ok(self.cu.cuModuleLoad(C.byref(self.mod), cubin.encode()), "cuModuleLoad")
-        cnt = C.c_uint()
-        self._ok(self.cu.cuModuleGetFunctionCount(C.byref(cnt), self.mod), "count")
-        funcs = (C.c_void_p * cnt.value)()
-        self._ok(self.cu.cuModuleEnumerateFunctions(funcs, cnt, self.mod), "enumerate")
-        self.funcs = {}
-        for f in funcs:
-            name = C.c_char_p()
-            self._ok(self.cu.cuFuncGetName(C.byref(name), C.c_void_p(f)), "name")
-            self.funcs[name.value.decode()] = C.c_void_p(f)
-
-    @staticmethod
-    def _ok(rc, what):
-        if rc != 0:
-            raise RuntimeError("%s failed: CUresult %d" % (what, rc))
-
-    def func(self, short):
-        key = "%d%s" % (len(short), short)
-        hits = [n for n in self.funcs if n.startswith("_ZN6cubble" + key)]
-        if len(hits) != 1:
-            raise KeyError(short)
-        return self.funcs[hits[0]]
-
-    def global_ptr(self, short):
-        name = "_ZN6cubble%d%sE" % (len(short), short)
-        ptr, size = C.c_uint64(), C.c_size_t()
-        self._ok(self.cu.cuModuleGetGlobal_v2(C.byref(ptr), C.byref(size), self.mod,
-                                              name.encode()), name)
-        return ptr.value, size.value
-
-    def get_global(self, short, ctype):
-        p, _ = self.global_ptr(short)
-        v = ctype()
-        self.sync()
-        self._ok(self.cu.cuMemcpyDtoH_v2(C.byref(v), C.c_uint64(p), C.sizeof(v)), "DtoH")
-        return v.value
-
-    def set_global(self, short, value):
-        p, _ = self.global_ptr(short)
-        self._ok(self.cu.cuMemcpyHtoD_v2(C.c_uint64(p), C.byref(value), C.sizeof(value)), "HtoD")
-
-    def launch(self, short, args, smem=0):
-        params = (C.c_void_p * len(args))(*[C.cast(C.pointer(a), C.c_void_p) for a in args])
-        self._ok(self.cu.cuLaunchKernel(self.func(short), GRID, 1, 1, BLOCK, 1, 1, smem, None,
-                                        params, None), short)
-
-    def sync(self):
-        self._ok(self.cu.cuCtxSynchronize(), "sync")
-
-
-class Foam:
-    """The reference's device state for one foam (Bubbles rows, pairs,
-    temporaries), in torch device buffers."""
-
-    def __init__(self, drv, cfg, n, pair_stride):
-        t = drv.torch
-        self.drv, self.cfg, self.n = drv, cfg, n
-        self.stride = n + (32 - n % 32) % 32
-        dev = "cuda"
-        self.d = {k: t.zeros(self.stride, dtype=t.float64, device=dev) for k in DROWS}
-        self.i = {k: t.zeros(self.stride, dtype=t.int32, device=dev) for k in IROWS}
-        self.pstride = pair_stride
-        self.pi = t.zeros(pair_stride, dtype=t.int32, device=dev)
-        self.pj = t.zeros(pair_stride, dtype=t.int32, device=dev)
-        self.tmpi = t.zeros(max(self.stride, 1) * 2, dtype=t.int32, device=dev)
-        self.tempD1 = t.zeros(self.stride, dtype=t.float64, device=dev)
-        self.blockMax = t.zeros(3 * GRID, dtype=t.float64, device=dev)
-        self.const = t.zeros(C.sizeof(Constants), dtype=t.uint8, device=dev)
-        self.np = 0
-        k = Constants()
-        dim = cfg.dimensionality
-        k.lbb = DVec(*cfg.lbb)
-        k.tfr = DVec(*cfg.tfr)
-        k.interval = DVec(*[cfg.tfr[a] - cfg.lbb[a] for a in range(3)])
-        k.flowLbb = DVec(*cfg.flow_lbb)
-        k.flowTfr = DVec(*cfg.flow_tfr)
-        k.flowVel = DVec(*cfg.flow_vel)
-        k.averageSurfaceAreaIn = cfg.average_surface_area_in
-        k.minRad = cfg.min_rad
-        k.fZeroPerMuZero = cfg.f0_per_mu0
-        k.kParameter = cfg.k_parameter
-        k.kappa = cfg.kappa
-        k.wallDragStrength = cfg.wall_drag
-        k.skinRadius = cfg.skin_radius
-        k.bubbleVolumeMultiplier = cfg.bubble_volume_multiplier
-        k.dimensionality = dim
-        k.xWall, k.yWall, k.zWall = (bool(w) for w in cfg.wall)
-        host = t.frombuffer(bytearray(bytes(k)), dtype=t.uint8)
-        self.const.copy_(host)
-        drv.set_global("dConstants", C.c_uint64(self.const.data_ptr()))
-        drv.set_global("dNumPairs", C.c_int32(0))
-        drv.launch("initGlobals", [])
-
-    def bubbles(self):
-        b = Bubbles()
-        for k in DROWS:
-            setattr(b, k, self.d[k].data_ptr())
-        for k in IROWS:
-            setattr(b, k, self.i[k].data_ptr())
-        b.count = self.n
-        b.stride = self.stride
-        b.numDP, b.numIP = 30, 5
-        return b
-
-    def pairs(self):
-        p = Pairs()
-        p.i, p.j = self.pi.data_ptr(), self.pj.data_ptr()
-        p.count = self.np
-        p.stride = self.pstride
-        return p
-
-    def put(self, key, arr):
-        t = self.drv.torch
-        src = t.from_numpy(np.ascontiguousarray(arr))
-        (self.d if key in self.d else self.i)[key][:len(arr)].copy_(src)
-
-    def get(self, key, n=None):
-        n = self.n if n is None else n
-        return (self.d if key in self.d else self.i)[key][:n].cpu().numpy().copy()
-
-    def set_pairs(self, i, j):
-        t = self.drv.torch
-        self.pi[:len(i)].copy_(t.from_numpy(np.asarray(i, np.int32)))
-        self.pj[:len(j)].copy_(t.from_numpy(np.asarray(j, np.int32)))
-        self.np = len(i)
-        self.drv.set_global("dNumPairs", C.c_int32(self.np))
-
-    def swap(self, a, b):
-        self.d[a], self.d[b] = self.d[b], self.d[a]
-
-
-def load(f, st):
-    for k_ref, k_st in (("x", "x"), ("y", "y"), ("z", "z"), ("r", "r"),
-                        ("dxdt", "dxdt"), ("dydt", "dydt"), ("dzdt", "dzdt"), ("drdt", "drdt"),
-                        ("dxdto", "dxdto"), ("dydto", "dydto"), ("dzdto", "dzdto"),
-                        ("drdto", "drdto"), ("path", "path"), ("error", "error"),
-                        ("savedX", "saved_x"), ("savedY", "saved_y"), ("savedZ", "saved_z"),
-                        ("savedR", "saved_r")):
-        if k_st in st:
-            f.put(k_ref, st[k_st])
-    for k_ref, k_st in (("index", "index"), ("numNeighbors", "num_neighbors")):
-        if k_st in st:
-            f.put(k_ref, st[k_st].astype(np.int32))
-    f.put("rp", st["r"])  # rp == r before the first step (src/simulator.cu:737-742)
+from oracle.ref.harness import (BLOCK, CUBIN, DROWS, GRID, IROWS, Constants,  # noqa: E402,F401
+                                Driver, DVec, Foam, IVec, load)
 
 
 # ------------------------------------------------------------------ flows
@@ -352,12 +166,12 @@ def ref_bootstrap(drv, cfg, st, pi, pj, ts):
     return {k: f.get(k) for k in ("dxdto", "dydto", "dzdto")}
 
 
-def ref_delete(drv, cfg, st, pi, pj, ts):
+def ref_delete(drv, cfg, st, pi, pj, ts, flow=False):
     """An accepted attempt with deletions: rotation of integrate()
     (src/simulator.cu:258-301) then removeBubbles() with the deletion list
     in ascending order."""
     n = len(st["x"])
-    f, out = ref_attempt(drv, cfg, st, pi, pj, ts)
+    f, out = ref_attempt(drv, cfg, st, pi, pj, ts, flow=flow)
     for a, b in (("x", "xp"), ("y", "yp"), ("z", "zp"), ("r", "rp"), ("path", "pathNew")):
         f.swap(a, b)
     for ax in ("x", "y", "z", "r"):
@@ -447,15 +261,44 @@ def ref_init(drv, dim, seed):
 
 
 # ------------------------------------------------------------------ cases
+def flow_box(cfg, frac_lo, frac_hi, vel):
+    """Sets the imposed-flow region to the fraction [frac_lo, frac_hi] of the
+    box on every axis of the foam and its velocity to `vel` (already scaled
+    by f0/mu0, as after src/simulator.cu:569-570)."""
+    dim = cfg.dimensionality
+    lo, hi = [0.0, 0.0, 0.0], [0.0, 0.0, 0.0]
+    for a in range(dim):
+        L = cfg.tfr[a] - cfg.lbb[a]
+        lo[a] = cfg.lbb[a] + frac_lo[a] * L
+        hi[a] = cfg.lbb[a] + frac_hi[a] * L
+    cfg.use_flow = 1
+    for a in range(3):
+        cfg.flow_lbb[a], cfg.flow_tfr[a] = lo[a], hi[a]
+        cfg.flow_vel[a] = vel[a] if a < dim else 0.0
+    return cfg
+
+
 def cases():
+    """(name, (config, state)) of every recorded foam. The flow cases run the
+    reference's box flow: pairwiseInteraction's neighbour-velocity sums
+    (src/kernels.cu:191-208, :281-283) and addFlowVelocity
+    (src/kernels.cu:497-544) in every attempt and in the deletion step."""
     from cubble_gb300 import workloads
     out = []
-    out.append(("2d", workloads.foam(1200, 2, 0.9, seed=501, min_rad=0.05), {}))
-    out.append(("3d", workloads.foam(1500, 3, 0.8, rstd=0.15, rclip=(0.3, 2.5), seed=502), {}))
+    out.append(("2d", workloads.foam(1200, 2, 0.9, seed=501, min_rad=0.05)))
+    out.append(("3d", workloads.foam(1500, 3, 0.8, rstd=0.15, rclip=(0.3, 2.5), seed=502)))
     out.append(("2d_wallx", workloads.foam(1000, 2, 0.85, seed=503, wall=(1, 0, 0),
-                                           wall_drag=0.2), {}))
+                                           wall_drag=0.2)))
     out.append(("3d_wallz", workloads.foam(1200, 3, 0.8, seed=504, wall=(0, 0, 1),
-                                           wall_drag=0.1), {}))
+                                           wall_drag=0.1)))
+    cfg, st = workloads.foam(1200, 2, 0.9, seed=505, min_rad=0.05)
+    out.append(("2d_flow", (flow_box(cfg, (0.0, 0.3, 0.0), (1.0, 0.6, 0.0),
+                                     (0.02, -0.005, 0.0)), st)))
+    cfg, st = workloads.foam(1500, 3, 0.8, rstd=0.15, rclip=(0.3, 2.5), seed=506)
+    out.append(("3d_flow", (flow_box(cfg, (0.2, 0.0, 0.4), (0.7, 1.0, 0.8),
+                                     (0.01, 0.004, -0.003)), st)))
+    # the 2D configuration at its stated size: N = 10^4, phi 0.90, min_rad 0.05
+    out.append(("2d_c1", workloads.config_c1(seed=507)))
     return out
 
 
@@ -469,10 +312,13 @@ def oracle_pairs(cfg, st):
     return s, i, j
 
 
-def main(out_dir):
+def main(out_dir, only=None):
     os.makedirs(out_dir, exist_ok=True)
     drv = Driver(CUBIN)
-    for name, (cfg, st), _ in cases():
+    for name, (cfg, st) in cases():
+        if only and name not in only:
+            continue
+        flow = bool(cfg.use_flow)
         rng = np.random.default_rng(7)
         n = len(st["x"])
         data = {"cfg_" + f: np.array(getattr(cfg, f)) for f, _ in type(cfg)._fields_}
@@ -508,7 +354,7 @@ def main(out_dir):
             data["attempt_in_" + k] = v
         data["attempt_pi"], data["attempt_pj"] = pi, pj
         data["attempt_ts"] = np.array(ts)
-        _, out = ref_attempt(drv, cfg, st_a, pi, pj, ts)
+        _, out = ref_attempt(drv, cfg, st_a, pi, pj, ts, flow=flow)
         for k, v in out.items():
             data["attempt_out_" + k] = v
         # 3. bootstrap
@@ -530,7 +376,7 @@ def main(out_dir):
         st_d["error"] = np.zeros(n)
         for k, v in st_d.items():
             data["delete_in_" + k] = v
-        res = ref_delete(drv, cfg, st_d, pi, pj, 1e-5)
+        res = ref_delete(drv, cfg, st_d, pi, pj, 1e-5, flow=flow)
         for k, v in res.items():
             data["delete_out_" + k] = v
         path = os.path.join(out_dir, "ref_%s.npz" % name)
@@ -548,9 +394,15 @@ def main_init(out_dir):
 
 
 if __name__ == "__main__":
-    args = [a for a in sys.argv[1:] if a != "--init"]
-    out = args[0] if args else os.path.join(ROOT, "gpurun_out", "golden")
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    if len(args) != 1:
+        raise SystemExit("usage: make_golden.py [--init] [--only=NAME,...] OUT_DIR")
+    out = args[0]
+    only = None
+    for a in sys.argv[1:]:
+        if a.startswith("--only="):
+            only = set(a[len("--only="):].split(","))
     if "--init" in sys.argv:
         main_init(out)
     else:
-        main(out)
+        main(out, only)
