@@ -359,6 +359,24 @@ def measure_form(args, world, rank, precision, clocks_on=True):
     bs_all = allreduce(bs, _op("sum"), world)
     np_per_n = r1["num_pairs"] / max(r1["count"], 1)
     kms = sim.profile_kernels(reps=5)
+    # the steady-state rate with its searches: a longer run continuing from
+    # the timed steps (integrate() searches when the largest expansion since
+    # the last search reaches half the skin), and the device time of one
+    # search of the current state
+    amort = None
+    if args.amortised_steps > 0:
+        qa0 = sim.report()
+        qa1, ams = sim.integrate_timed(args.amortised_steps)
+        na = qa1["steps"] - qa0["steps"]
+        sa = qa1["searches"] - qa0["searches"]
+        amort = {"value": (qa1["bubble_steps"] - qa0["bubble_steps"]) / (ams / 1e3),
+                 "unit": "bubble-steps/s", "steps": na, "ms_per_step": ams / max(na, 1),
+                 "attempts": qa1["attempts"] - qa0["attempts"], "searches": sa,
+                 "deleted": qa1["deleted"] - qa0["deleted"],
+                 "steps_per_search": (na / sa) if sa else None,
+                 "what": "%d accepted steps after the timed ones, searches and deletions "
+                         "included, one graph launch, CUDA events" % na}
+    search_ms = sim.profile_search(reps=3)
     names = ["predict", "pairs", "correct"]
     top = int(np.argmax(kms))
     mixed = precision == 1
@@ -400,7 +418,7 @@ def measure_form(args, world, rank, precision, clocks_on=True):
     sim.close()
     return {"value": bs_all / el, "el": el, "cfg": cfg, "st": st, "desc": desc, "r0": r0,
             "r1": r1, "roofline": roof, "launches": launches, "clocks": clk,
-            "np_per_n": np_per_n}
+            "np_per_n": np_per_n, "amortised": amort, "search_ms": search_ms}
 
 
 def form_errors(args, precision=1, steps=50):
@@ -467,11 +485,103 @@ def form_errors(args, precision=1, steps=50):
     return out
 
 
+def _attempt_errors(ga, gb, s, tol):
+    """Largest per-row error of attempt `gb` against attempt `ga` from state
+    `s`: positions and radii by their change over the attempt, rates and
+    overlap areas by each row's largest magnitude, the error estimate
+    relative to the tolerance it is compared with."""
+    def rel(x, y):
+        return float(np.max(np.abs(x - y)) / max(np.max(np.abs(y)), 1e-300))
+    e = {}
+    for k, base in (("xp", "x"), ("yp", "y"), ("zp", "z"), ("rp", "r")):
+        e["d" + base] = rel(gb[k] - s[base], ga[k] - s[base])
+    for k in ("dxdtp", "dydtp", "dzdtp", "drdtp", "overlap", "path_new"):
+        e[k] = rel(gb[k], ga[k])
+    e["max_error_vs_tol"] = abs(gb["max_error"] - ga["max_error"]) / tol
+    e["max_error_rel"] = abs(gb["max_error"] / ga["max_error"] - 1.0)
+    return e
+
+
+def long_horizon_errors(args, steps, every):
+    """The mixed form against the FP64 form over `steps` accepted steps from
+    the same prepared state (the survey's C3 beside C2). Every `every`
+    steps: both runs' energies (the energy-decay curve), the mixed run's
+    total gas volume against the FP64 run's, and the mixed form's per-step
+    error measured on the FP64 run's own state (one attempt of each form
+    from that state, `_attempt_errors`)."""
+    import cubble_gb300 as cb
+    from cubble_gb300 import workloads
+    cfg64, st, _ = workload(args.workload, args.seed, precision=0, use_graph=1)
+    cfgmx, _, _ = workload(args.workload, args.seed, precision=1, use_graph=1)
+    a = cb.GpuFoam(cfg64)
+    a.load_state(st)
+    workloads.prepare(a)
+    a.integrate(args.warmup)
+    s0 = a.get_state()
+    i0, j0 = a.pairs()
+    dt = a.report()["time_step"]
+    b = cb.GpuFoam(cfgmx)
+    b.load_state(s0)
+    b.set_pairs(i0, j0)
+    b.set_time(dt)
+    a.set_time(dt)
+    p64, pmx = cb.GpuFoam(cfg64), cb.GpuFoam(cfgmx)
+    tol = cfg64.error_tolerance
+    v0 = a.total_volume()
+    ra0, rb0 = a.report(), b.report()
+    curve, worst = [], {}
+    done = 0
+    while True:
+        sa = a.get_state()
+        ia, ja = a.pairs()
+        q = a.report()
+        for f in (p64, pmx):
+            f.load_state(sa)
+            f.set_pairs(ia, ja)
+            f.set_time(q["time_step"])
+        err = _attempt_errors(p64.attempt(), pmx.attempt(), sa, tol)
+        for k, v in err.items():
+            worst[k] = max(worst.get(k, 0.0), v)
+        ea, eb = a.energy(), b.energy()
+        curve.append({"step": done, "energy_fp64": ea, "energy_mixed": eb,
+                      "energy_rel": abs(eb / ea - 1.0),
+                      "volume_drift": abs(b.total_volume() / a.total_volume() - 1.0),
+                      "per_step_max": max(v for k, v in err.items() if k != "max_error_rel")})
+        if done >= steps:
+            break
+        a.integrate(every)
+        b.integrate(every)
+        done += every
+    ra, rb = a.report(), b.report()
+    out = {"steps": done, "sample_every": every,
+           "same_attempts_searches_deletions": all(
+               ra[k] - ra0[k] == rb[k] - rb0[k] for k in ("attempts", "searches", "deleted")),
+           "counts_fp64": {k: ra[k] - ra0[k] for k in ("attempts", "searches", "deleted")},
+           "counts_mixed": {k: rb[k] - rb0[k] for k in ("attempts", "searches", "deleted")},
+           "volume_drift": abs(b.total_volume() / a.total_volume() - 1.0),
+           "volume_change_fp64": a.total_volume() / v0 - 1.0,
+           "energy_rel_end": curve[-1]["energy_rel"],
+           "per_step_worst": worst, "curve": curve,
+           "reference": "the FP64 form of this library (equal to the FP64 oracle within "
+                        "1e-12 per step) on the same input",
+           "error_definition": "per step: one attempt of each form from the FP64 run's state "
+                               "every sample; max over bubbles |mixed - fp64| / max |fp64| per "
+                               "row (positions, radii: their change over the attempt); the error "
+                               "estimate relative to the tolerance (max_error_vs_tol) and to "
+                               "itself (max_error_rel, a difference of nearly equal FP32 rates)"}
+    for f in (a, b, p64, pmx):
+        f.close()
+    return out
+
+
 def batch_errors(items, steps=50):
     """Mixed batch against the FP64 batch of the same foams from the same
     FP64-prepared state (positions, rates, pairs, dt): max over foams of the
     displacement-relative position error, the radius error and the total
-    volume drift after `steps` accepted steps."""
+    volume drift after `steps` accepted steps. Over thousands of steps the
+    two runs of a chaotic foam part (a deletion may land a step apart), so
+    positions and radii are compared on the bubbles both runs still hold;
+    the total gas volume is what stays comparable."""
     import cubble_gb300 as cb
     from cubble_gb300 import workloads
     cf64 = [c for c, _ in items]
@@ -489,21 +599,27 @@ def batch_errors(items, steps=50):
         s0.append(s)
     r64, rmx = b64.integrate(steps), bmx.integrate(steps)
     out = {"steps": steps, "foams": len(items), "same_attempts_searches_deletions": True,
-           "dx": 0.0, "r": 0.0, "volume_drift": 0.0}
+           "foams_with_same_counts": 0, "dx": 0.0, "r": 0.0, "volume_drift": 0.0,
+           "deleted_fp64": 0, "deleted_mixed": 0}
     for f, ((cfg, _), f64, fmx) in enumerate(zip(items, b64.foams, bmx.foams)):
-        if any(r64[f][k] != rmx[f][k] for k in ("attempts", "searches", "deleted")):
-            out["same_attempts_searches_deletions"] = False
+        same = all(r64[f][k] == rmx[f][k] for k in ("attempts", "searches", "deleted"))
+        out["same_attempts_searches_deletions"] &= same
+        out["foams_with_same_counts"] += int(same)
+        out["deleted_fp64"] += r64[f]["deleted"]
+        out["deleted_mixed"] += rmx[f]["deleted"]
         a, b = f64.get_state(), fmx.get_state()
-        order_a, order_b = np.argsort(a["index"]), np.argsort(b["index"])
-        o0 = np.argsort(s0[f]["index"])
+        common = np.intersect1d(a["index"], b["index"])
+        pa = np.argsort(a["index"])[np.searchsorted(np.sort(a["index"]), common)]
+        pb = np.argsort(b["index"])[np.searchsorted(np.sort(b["index"]), common)]
+        p0 = np.argsort(s0[f]["index"])[np.searchsorted(np.sort(s0[f]["index"]), common)]
         for ax, k in enumerate(("x", "y")):
             L = cfg.tfr[ax] - cfg.lbb[ax]
-            d = b[k][order_b] - a[k][order_a]
+            d = b[k][pb] - a[k][pa]
             d -= L * np.round(d / L)
-            m = a[k][order_a] - s0[f][k][o0]
+            m = a[k][pa] - s0[f][k][p0]
             m -= L * np.round(m / L)
             out["dx"] = max(out["dx"], float(np.max(np.abs(d)) / max(np.max(np.abs(m)), 1e-300)))
-        out["r"] = max(out["r"], float(np.max(np.abs(b["r"][order_b] - a["r"][order_a])) /
+        out["r"] = max(out["r"], float(np.max(np.abs(b["r"][pb] - a["r"][pa])) /
                                         np.max(np.abs(a["r"]))))
         v64, vmx = f64.total_volume(), fmx.total_volume()
         out["volume_drift"] = max(out["volume_drift"], abs(vmx - v64) / v64)
@@ -569,7 +685,76 @@ def measure_batch(args, world, rank):
         pick = sorted(range(len(items)), key=lambda f: items[f][1]["x"].size)
         sub = [items[f] for f in pick[:: max(1, len(pick) // 4)][:4]]
         sub = [(workloads.sweep_config_as(c, precision=0), st) for c, st in sub]
-        out["error_vs_fp64"] = batch_errors(sub)
+        out["error_vs_fp64"] = batch_errors(sub, steps=args.batch_error_steps)
+    return out
+
+
+def reference_cuda(args, steps):
+    """The reference's own CUDA step loop on the same GB300: KJLankinen/cubble's
+    src/kernels.cu compiled unmodified for sm_103a (oracle/ref/build_ref.py),
+    driven by oracle/ref/harness.py's restatement of integrate()
+    (src/simulator.cu:60-337: per attempt four launches and the blocking
+    copy of the block maxima, host dt decision, pointer rotation, searches
+    and deletions). It starts from this library's prepared foam (state, pair
+    list, dt); this library's FP64 and mixed forms run the same `steps`
+    accepted steps from the same state. A reported baseline, never the
+    measured path: the harness runs only here and in the golden-vector
+    recorder."""
+    import torch
+    import cubble_gb300 as cb
+    from cubble_gb300 import workloads
+    from oracle.ref import harness
+    if not os.path.exists(harness.CUBIN):
+        return {"unavailable": "reference cubin oracle/_ref/kernels_ref.cubin not built "
+                               "(the reference sources were absent when build() ran)"}
+    cfg, st, desc = workload(args.workload, args.seed, precision=0, use_graph=1)
+    g = cb.GpuFoam(cfg)
+    g.load_state(st)
+    workloads.prepare(g)
+    g.integrate(args.warmup)
+    s = g.get_state()
+    pi, pj = g.pairs()
+    rep = g.report()
+    g.close()
+    dt, max_r = rep["time_step"], rep["max_radius"]
+    drv = harness.Driver(harness.CUBIN)
+    warm = harness.RefSim(drv, cfg, s, pi, pj, dt, max_r)
+    warm.integrate(3)  # loads the kernels' code; the timed run starts afresh
+    drv.sync()
+    del warm
+    sim = harness.RefSim(drv, cfg, s, pi, pj, dt, max_r)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    e0.record()
+    sim.integrate(steps)
+    e1.record()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    ref_ms = e0.elapsed_time(e1)
+    out = {"value": sim.bubble_steps / (ref_ms / 1e3), "unit": "bubble-steps/s",
+           "steps": steps, "ms_per_step": ref_ms / steps, "wall_s": wall,
+           "attempts": sim.attempts, "searches": sim.searches, "deleted": sim.deleted,
+           "what": "the reference's src/kernels.cu (unmodified, sm_103a) under its own "
+                   "integrate() host loop, from the same prepared foam; CUDA events on the "
+                   "default stream around the whole loop (host round trips included)"}
+    forms = {}
+    for prec, name in ((0, "fp64"), (1, "mixed")):
+        cfgp, _, _ = workload(args.workload, args.seed, precision=prec, use_graph=1)
+        f = cb.GpuFoam(cfgp)
+        f.load_state(s)
+        f.set_pairs(pi, pj)
+        f.set_time(dt)
+        q0 = f.report()
+        q1, ms = f.integrate_timed(steps)
+        forms[name] = {"value": (q1["bubble_steps"] - q0["bubble_steps"]) / (ms / 1e3),
+                       "ms_per_step": ms / steps,
+                       "attempts": q1["attempts"] - q0["attempts"],
+                       "searches": q1["searches"] - q0["searches"],
+                       "deleted": q1["deleted"] - q0["deleted"]}
+        forms[name]["speedup_vs_reference_cuda"] = forms[name]["value"] / out["value"]
+        f.close()
+    out["gb300"] = forms
     return out
 
 
@@ -590,19 +775,26 @@ def run_gb300(args, world, rank, local):
     e2e = None
     if not args.no_e2e:
         host, keep = pinned_copy(st)
+        down, keep_down = pinned_copy({k: np.zeros_like(v) for k, v in st.items()})
         g2 = cb.GpuFoam(cfg)
         barrier(world)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         g2.load_state(host)
+        t1 = time.perf_counter()
         workloads.prepare(g2)
+        t2 = time.perf_counter()
         q0 = g2.report()
         for _ in range(args.warmup + args.steps):
             g2.integrate(1)
         q1 = g2.report()
-        fin = g2.get_state(rows=list(host.keys()))
+        t3 = time.perf_counter()
+        fin = g2.get_state(rows=list(host.keys()), out=down)
         torch.cuda.synchronize()
-        e2e_s = time.perf_counter() - t0
+        t4 = time.perf_counter()
+        e2e_s = t4 - t0
+        parts = {"upload_ms": 1e3 * (t1 - t0), "search_bootstrap_ms": 1e3 * (t2 - t1),
+                 "steps_ms": 1e3 * (t3 - t2), "download_ms": 1e3 * (t4 - t3)}
         barrier(world)
         e2e_s = allreduce(e2e_s, _op("max"), world)
         e2e_bs = allreduce(q1["bubble_steps"] - q0["bubble_steps"], _op("sum"), world)
@@ -612,10 +804,11 @@ def run_gb300(args, world, rank, local):
         e2e = {"value": e2e_bs / e2e_s, "unit": "bubble-steps/s",
                "h2d_bytes_per_step": state_bytes(host) // nsteps,
                "d2h_bytes_per_step": rep + state_bytes(fin) // nsteps,
-               "steps": nsteps, "note": "state upload, search, bootstrap, %d steps each reading "
-                                         "its report back, state download" % nsteps}
+               "steps": nsteps, "host_wall_ms": parts,
+               "note": "state upload, search, bootstrap, %d steps each reading "
+                       "its report back, state download (pinned host buffers)" % nsteps}
         g2.close()
-        del keep
+        del keep, keep_down
 
     mixed = None
     if args.precision == 0 and not args.no_mixed:
@@ -631,6 +824,11 @@ def run_gb300(args, world, rank, local):
                              "volume sum and fix, error norm, energy"}
         if rank == 0:
             mixed["error_vs_fp64"] = form_errors(args, 1)
+            if args.long_steps > 0:
+                mixed["long_horizon_vs_fp64"] = long_horizon_errors(args, args.long_steps,
+                                                                    args.long_every)
+        mixed["amortised"] = mx["amortised"]
+        mixed["search_ms"] = mx["search_ms"]
 
     fp64_ff = None
     if args.precision == 0 and not args.no_ff:
@@ -651,6 +849,13 @@ def run_gb300(args, world, rank, local):
     batched = None
     if not args.no_batch:
         batched = measure_batch(args, world, rank)
+
+    ref_cuda = None
+    if rank == 0 and args.ref_cuda_steps > 0:
+        try:
+            ref_cuda = reference_cuda(args, args.ref_cuda_steps)
+        except Exception as e:  # the baseline is reported, never required
+            ref_cuda = {"unavailable": "%s: %s" % (type(e).__name__, e)}
 
     base = None
     if rank == 0 and not args.no_cpu:
@@ -675,6 +880,10 @@ def run_gb300(args, world, rank, local):
                    "steps_per_search": (args.steps / searches) if searches else None,
                    "pairs_per_bubble": main["np_per_n"], "bubbles_end": r1["count"],
                    "deleted": r1["deleted"] - r0["deleted"], "dt_end": r1["time_step"]},
+        "search": {"search_ms": main["search_ms"],
+                   "what": "device time of one neighbour search of the N-bubble foam "
+                           "(CUDA events, mean of 3)"},
+        "amortised": main["amortised"], "reference_cuda": ref_cuda,
         "roofline": main["roofline"], "cpu_baseline": base, "e2e": e2e,
         "gpu_launches": main["launches"], "clocks": main["clocks"], "mixed": mixed,
         "fp64_ff": fp64_ff, "batched": batched,
@@ -707,6 +916,17 @@ def main():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-ff", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    # accepted steps of the search-inclusive run after the timed ones (0: off)
+    ap.add_argument("--amortised-steps", type=int, default=500)
+    # accepted steps of the reference's CUDA step loop and of both forms from
+    # the same state (0: off)
+    ap.add_argument("--ref-cuda-steps", type=int, default=200)
+    # the mixed form against the FP64 form over this many steps (0: off),
+    # sampled every --long-every steps; the batched sweep's mixed-vs-FP64
+    # drift over --batch-error-steps steps per foam
+    ap.add_argument("--long-steps", type=int, default=2000)
+    ap.add_argument("--long-every", type=int, default=100)
+    ap.add_argument("--batch-error-steps", type=int, default=5000)
     ap.add_argument("--until-deleted", type=float, default=0.0)
     ap.add_argument("--chunk-steps", type=int, default=2000)
     ap.add_argument("--max-run-steps", type=int, default=200000)

@@ -60,6 +60,12 @@ class GpuFoam(Foam):
         self._call("profile_kernels", self._ctx, int(reps), ms)
         return tuple(ms)
 
+    def profile_search(self, reps=3):
+        """Mean device ms of one neighbour search of the current state."""
+        ms = C.c_double()
+        self._call("profile_search", self._ctx, int(reps), C.byref(ms))
+        return ms.value
+
     def launch_count(self):
         n = C.c_int64()
         self._call("launch_count", self._ctx, C.byref(n))
@@ -167,6 +173,12 @@ class GpuFoamBatch:
         t = C.c_int32()
         self._call("batch_autotune", self._b, int(steps_per_trial), C.byref(t))
         return t.value
+
+    def profile_search(self, reps=3):
+        """Mean device ms of one neighbour search of the current state."""
+        ms = C.c_double()
+        self._call("profile_search", self._ctx, int(reps), C.byref(ms))
+        return ms.value
 
     def launch_count(self):
         n = C.c_int64()

@@ -151,6 +151,7 @@ def declare(lib, prefix):
                                           C.POINTER(C.c_double)]),
             "launch_count": (C.c_int, [vp, C.POINTER(C.c_int64)]),
             "profile_kernels": (C.c_int, [vp, C.c_int32, C.POINTER(C.c_double)]),
+            "profile_search": (C.c_int, [vp, C.c_int32, C.POINTER(C.c_double)]),
             "energy_noalloc": (C.c_int, [C.POINTER(Config), vp, vp, vp, vp, vp, vp,
                                          C.c_int32, C.c_int32, vp, vp]),
             "integrate_until": (C.c_int, [vp, C.c_int64, C.POINTER(Stop), C.POINTER(Report)]),

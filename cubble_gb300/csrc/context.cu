@@ -962,6 +962,30 @@ int cb_profile_kernels(cb_context *c, int32_t reps, double ms[3]) {
     return c->push();
 }
 
+int cb_profile_search(cb_context *c, int32_t reps, double *ms) {
+    NvtxRange nv("Neighbors");
+    CB_ENTER(c);
+    if (!c->loaded) return fail(CB_ERR_STATE, "state not loaded");
+    if (reps < 1 || !ms) return fail(CB_ERR_INVALID_ARGUMENT, "bad arguments");
+    int rc = c->pull();
+    if (rc) return rc;
+    const long long searches0 = c->hctrl->searches;
+    // one search untimed: the first launch of a kernel also loads its code
+    if ((rc = run_search(c))) return rc;
+    CB_CUDA(cudaStreamSynchronize(c->stream));
+    CB_CUDA(cudaEventRecord(c->ev0, c->stream));
+    for (int r = 0; r < reps; r++) launch_search(c->launch, c->bufs, c->hk.dim);
+    CB_CUDA(cudaEventRecord(c->ev1, c->stream));
+    CB_CUDA(cudaEventSynchronize(c->ev1));
+    float t = 0.f;
+    CB_CUDA(cudaEventElapsedTime(&t, c->ev0, c->ev1));
+    *ms = (double)t / reps;
+    if ((rc = c->check_launch())) return rc;
+    if ((rc = sync_status(c))) return rc;
+    c->hctrl->searches = searches0;  // measurement searches are not the run's
+    return c->push();
+}
+
 int cb_launch_count(cb_context *c, int64_t *count) {
     if (!c || !count) return fail(CB_ERR_INVALID_ARGUMENT, "null argument");
     *count = c->launches;

@@ -122,20 +122,31 @@ class Foam:
     def count(self):
         return self.report()["count"]
 
-    def get_state(self, rows=None):
+    def get_state(self, rows=None, out=None):
+        """The persistent rows (all, or `rows`) as numpy arrays; `out` may
+        give the destination arrays (e.g. pinned host buffers, each holding at
+        least count() elements of the row's type)."""
         n = self.count()
-        out = {}
+        res = {}
         v = _abi.StateView()
         for k in DROWS:
             if rows is None or k in rows:
-                out[k] = np.zeros(n, np.float64)
-                setattr(v, k, _dptr(out[k]))
+                if out is not None and k in out:
+                    res[k] = out[k][:n]
+                    assert res[k].dtype == np.float64 and res[k].flags.c_contiguous, k
+                else:
+                    res[k] = np.zeros(n, np.float64)
+                setattr(v, k, _dptr(res[k]))
         for k in IROWS:
             if rows is None or k in rows:
-                out[k] = np.zeros(n, np.int32)
-                setattr(v, k, _iptr(out[k]))
+                if out is not None and k in out:
+                    res[k] = out[k][:n]
+                    assert res[k].dtype == np.int32 and res[k].flags.c_contiguous, k
+                else:
+                    res[k] = np.zeros(n, np.int32)
+                setattr(v, k, _iptr(res[k]))
         self._call("get_state", self._ctx, C.byref(v))
-        return out
+        return res
 
     def set_options(self, use_gas_exchange, use_flow, increment_path):
         self._call("set_options", self._ctx, int(use_gas_exchange),
