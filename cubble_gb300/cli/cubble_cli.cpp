@@ -20,6 +20,9 @@
 //   --checkpoint FILE        write the full state at every printed time unit
 //   --resume FILE            continue a run from such a checkpoint
 //   --max-steps N            stop after N integration steps (testing)
+//   --output-digits N        significant digits of results.dat and the
+//                            snapshots (default 6, the reference's default
+//                            stream precision; 17 round-trips a double)
 //   --array FILE             expand an array.params file
 //                            (scripts/triton/array_job.py:54-75) into one
 //                            run per parameter set, each in run_<k>/.
@@ -49,6 +52,9 @@
 namespace {
 
 constexpr double kPi = 3.1415926535897932384626433832795028841971693993;
+
+// Significant digits of the output files (--output-digits).
+int g_output_digits = 6;
 
 void check(int rc, const char *what) {
     if (rc != CB_OK)
@@ -397,6 +403,7 @@ void write_snapshot(const SnapData &s, const std::string &name, uint32_t num,
     ss << name << ".csv." << num;
     std::ofstream file(ss.str().c_str(), std::ios::out);
     if (!file.is_open()) return;
+    file.precision(g_output_digits);
     file << "x,y,z,r,vx,vy,vz,vtot,vr,path,energy,displacement,error,index\n";
     for (int32_t i = 0; i < s.count; ++i) {
         const int32_t ind = s.index[i];
@@ -629,6 +636,7 @@ void simulate(Run &r) {
             check(cb_averages(r.ctx, avg), "cb_averages");
             const double rel_rad = avg[0] / r.avg_rad;
             std::ofstream res("results.dat", std::ios_base::app);
+            res.precision(g_output_digits);
             if (res.is_open()) {
                 const double vx = avg[1], vy = avg[2], vz = avg[3], vr = avg[4];
                 res << r.times_printed << " " << rel_rad << " " << rep.count << " " << avg[5] << " "
@@ -780,6 +788,10 @@ int main(int argc, char **argv) {
                 resume = next();
             } else if (s == "--max-steps") {
                 max_steps = std::stoll(next());
+            } else if (s == "--output-digits") {
+                g_output_digits = std::stoi(next());
+                if (g_output_digits < 1 || g_output_digits > 17)
+                    throw std::runtime_error("--output-digits must be 1 ... 17");
             } else if (s == "--array") {
                 array = next();
             } else if (input.empty()) {
