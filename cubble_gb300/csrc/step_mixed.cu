@@ -118,6 +118,13 @@ __device__ __forceinline__ float *acc_ov(const Bufs &b, int cap) {
 __device__ __forceinline__ float4 *acc_fl(const Bufs &b, int cap) {
     return reinterpret_cast<float4 *>(reinterpret_cast<float *>(b.acc) + 8 * (size_t)cap);
 }
+// The containment recheck list of the pair kernel (see k_pairs_mx) in the
+// unused bytes [48 cap, 64 cap) of the accumulators: element 0 holds the
+// count, then up to recheck_cap(cap) pairs (i, j). Zero between attempts.
+__device__ __forceinline__ int2 *recheck_list(float4 *AV, int cap) {
+    return reinterpret_cast<int2 *>(AV + 3 * (size_t)cap);
+}
+__device__ __forceinline__ int recheck_cap(int cap) { return min(1024 + cap / 128, 2 * cap - 1); }
 
 __device__ __forceinline__ void red_add4(float4 *p, float a, float b, float c, float d) {
     asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b),
@@ -242,6 +249,120 @@ CB_KERNEL_PAIR((template <int DIM>), k_predict_mx, (<DIM>), __launch_bounds__(kB
 
 
 // ------------------------------------------------------------------ pairs
+// FP32 geometry of a pair on exact fixed-point differences: the minimum image
+// on periodic axes (wrappedDifference, src/kernels.cu:1094-1114), the
+// differences as FP32 and the squared distance m.
+// Periodic axes and the fixed-point box (half) lengths, read once per kernel.
+struct FixBox {
+    bool px, py, pz;
+    long long hx, hy, hz, lx, ly, lz;
+};
+
+__device__ __forceinline__ FixBox fix_box(const DevConst &k, int dim) {
+    return {!k.wall[0], !k.wall[1], dim == 3 && !k.wall[2], k.hq[0], k.hq[1], k.hq[2],
+            k.lq[0], k.lq[1], k.lq[2]};
+}
+
+template <int DIM>
+__device__ __forceinline__ void pair_diff(const PredMx &a, const PredMx &q, const FixBox &f,
+                                          long long &ex, long long &ey, long long &ez,
+                                          float &dx, float &dy, float &dz, float &m) {
+    ex = a.q[0] - q.q[0];
+    ey = a.q[1] - q.q[1];
+    ez = 0;
+    if (f.px) ex = wrap_fix(ex, f.hx, f.lx);
+    if (f.py) ey = wrap_fix(ey, f.hy, f.ly);
+    if (DIM == 3) {
+        ez = a.q[2] - q.q[2];
+        if (f.pz) ez = wrap_fix(ez, f.hz, f.lz);
+    }
+    dx = len_from_fix(ex);
+    dy = len_from_fix(ey);
+    dz = DIM == 3 ? len_from_fix(ez) : 0.f;
+    m = dx * dx;
+    m = fmaf(dy, dy, m);
+    if (DIM == 3) m = fmaf(dz, dz, m);
+}
+
+// Overlap area of an overlapping pair (src/kernels.cu:236-256): min(r1, r2)^2
+// (3D, times pi) or 2 min(r1, r2) (2D) when one centre lies inside the other
+// bubble, else the lens formula.
+template <int DIM>
+__device__ __forceinline__ float overlap_area(float r1, float r2, float r1sq, float r2sq,
+                                              float m, float rs, bool inside) {
+    if (inside) return DIM == 3 ? fminf(r1sq, r2sq) * (float)kPi : 2.f * fminf(r1, r2);
+    const float tt = 0.5f * (r2sq - r1sq + m);
+    const float oa = fabsf(r2sq - (tt * tt) * (rs * rs));
+    return DIM == 3 ? oa * (float)kPi : 2.f * sqrtf(oa);
+}
+
+// The overlap area jumps where one centre enters the other bubble (at
+// d^2 = max(r1^2, r2^2) the lens formula gives r1^2 - r1^4 / (4 r2^2), the
+// containment branch r1^2: a step of pi r1^4 / (4 r2^2) in 3D). The FP32 test
+// can decide a pair within its rounding error of that threshold either way.
+// Such pairs (relative distance below kContainBand: a few per 10^6 bubbles
+// and attempt) are appended to a list; the last block of the pair kernel
+// decides them again in FP64 — on the exact fixed-point differences and on
+// both predicted radii recomputed from the state rows, r + h (3 v_r -
+// v_r,old), as the prediction defines them — and where the decision turns,
+// adds the difference of the two areas to both bubbles and to the global
+// sums before the mean-field factors are formed.
+constexpr float kContainBand = 3.814697265625e-06f;  // 2^-18
+
+__device__ __forceinline__ bool contained_exact(long long ex, long long ey, long long ez, int i,
+                                                int j, double *const *ds, const Ctrl *c) {
+    const double s = 9.094947017729282379e-13;  // 2^-40
+    const double dx = (double)ex * s, dy = (double)ey * s, dz = (double)ez * s;
+    const double m = dx * dx + dy * dy + dz * dz;
+    const double *R = ds[c->drole[RR]];
+    const float *V3 = reinterpret_cast<const float *>(ds[c->drole[RV3]]);
+    const float *O3 = reinterpret_cast<const float *>(ds[c->drole[RVO3]]);
+    const double h = (double)float_from_double(0.5 * c->dt);
+    const double r1 = R[i] + h * (double)fmaf(3.f, V3[i], -O3[i]);
+    const double r2 = R[j] + h * (double)fmaf(3.f, V3[j], -O3[j]);
+    return m < r1 * r1 || m < r2 * r2;
+}
+
+// Last block of the pair kernel: the listed pairs decided again (see above).
+// Returns this thread's changes of the summed overlap area and of the summed
+// area over radius.
+template <int DIM>
+__device__ __forceinline__ float2 recheck_containment(const int2 *RC, double *const *ds,
+                                                      const Ctrl *c, const DevConst *kp,
+                                                      const double *PB, float4 *AV, float *AO) {
+    const DevConst &k = *kp;
+    float so = 0.f, sor = 0.f;
+    const int cnt = min(RC[0].x, recheck_cap(k.cap));
+    const FixBox fb = fix_box(k, DIM);
+    for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+        const int2 pr = RC[1 + e];
+        const PredMx a = ld_pred(PB, pr.x), q = ld_pred(PB, pr.y);
+        long long ex, ey, ez;
+        float dx, dy, dz, m;
+        pair_diff<DIM>(a, q, fb, ex, ey, ez, dx, dy, dz, m);
+        const float r1 = a.r, r2 = q.r, r1sq = r1 * r1, r2sq = r2 * r2;
+        const bool fast = m < fmaxf(r1sq, r2sq);
+        const bool exact = contained_exact(ex, ey, ez, pr.x, pr.y, ds, c);
+        if (fast == exact) continue;
+        const float rs = rsqrtf(m);
+        const float d = overlap_area<DIM>(r1, r2, r1sq, r2sq, m, rs, exact) -
+                        overlap_area<DIM>(r1, r2, r1sq, r2sq, m, rs, fast);
+        const float dg = d * (q.inv - a.inv);
+        if (DIM == 3) {
+            atomicAdd(AO + pr.x, d);
+            atomicAdd(AO + pr.y, d);
+            red_add4(AV + pr.x, 0.f, 0.f, 0.f, dg);
+            red_add4(AV + pr.y, 0.f, 0.f, 0.f, -dg);
+        } else {
+            red_add4(AV + pr.x, 0.f, 0.f, d, dg);
+            red_add4(AV + pr.y, 0.f, 0.f, d, -dg);
+        }
+        so += d;
+        sor = fmaf(d, a.inv + q.inv, sor);
+    }
+    return make_float2(so, sor);
+}
+
 // The search emits the pairs grouped by i in ascending order, so consecutive
 // pairs mostly share their first bubble. Each thread takes a run of kRun
 // consecutive pairs (one 16-byte load of the i's and one of the j's), loads
@@ -264,9 +385,7 @@ __device__ __forceinline__ void k_pairs_mx_body(const Bufs &b, const int vb, con
     float *AO = acc_ov(b, cap);
     float4 *AF = acc_fl(b, cap);
     const float f0 = k.f0_f;
-    const bool px = !k.wall[0], py = !k.wall[1], pz = DIM == 3 && !k.wall[2];
-    const long long hx = k.hq[0], hy = k.hq[1], hz = k.hq[2];
-    const long long lx = k.lq[0], ly = k.lq[1], lz = k.lq[2];
+    const FixBox fb = fix_box(k, DIM);
     const double *PB = pred_base(b, c, cap);
     float sAo = 0.f, sAor = 0.f;
     const int nrun = (np + kRun - 1) / kRun;
@@ -319,19 +438,10 @@ __device__ __forceinline__ void k_pairs_mx_body(const Bufs &b, const int vb, con
             if (FLOW)  // src/kernels.cu:191-207 (added for every pair)
                 red_add4(AF + j, vxi, vyi, vzi, 0.f);
             const PredMx q = ld_pred(PB, j);
-            long long ex = a.q[0] - q.q[0], ey = a.q[1] - q.q[1], ez = 0;
-            if (px) ex = wrap_fix(ex, hx, lx);
-            if (py) ey = wrap_fix(ey, hy, ly);
-            if (DIM == 3) {
-                ez = a.q[2] - q.q[2];
-                if (pz) ez = wrap_fix(ez, hz, lz);
-            }
-            const float dx = len_from_fix(ex), dy = len_from_fix(ey);
-            const float dz = DIM == 3 ? len_from_fix(ez) : 0.f;
+            long long ex, ey, ez;
+            float dx, dy, dz, m;
+            pair_diff<DIM>(a, q, fb, ex, ey, ez, dx, dy, dz, m);
             const float r1 = a.r, r2 = q.r;
-            float m = dx * dx;
-            m = fmaf(dy, dy, m);
-            if (DIM == 3) m = fmaf(dz, dz, m);
             const float radii = r1 + r2;
             if (radii * radii >= m) {
                 // velocity f0 d (1/|d| - 1/(r1 + r2)), src/kernels.cu:218-233
@@ -341,13 +451,13 @@ __device__ __forceinline__ void k_pairs_mx_body(const Bufs &b, const int vb, con
                 float gf = 0.f, oa = 0.f;
                 if (GAS) {  // pairwise gas exchange, src/kernels.cu:236-280
                     const float r1sq = r1 * r1, r2sq = r2 * r2;
-                    if (m < r1sq || m < r2sq) {
-                        oa = DIM == 3 ? fminf(r1sq, r2sq) * (float)kPi : 2.f * fminf(r1, r2);
-                    } else {
-                        const float tt = 0.5f * (r2sq - r1sq + m);
-                        oa = fabsf(r2sq - (tt * tt) * (rs * rs));
-                        oa = DIM == 3 ? oa * (float)kPi : 2.f * sqrtf(oa);
+                    const float rm = fmaxf(r1sq, r2sq);
+                    if (fabsf(m - rm) <= kContainBand * rm) {  // decided again at the end
+                        int2 *RC = recheck_list(AV, cap);
+                        const int e = atomicAdd(&RC[0].x, 1);
+                        if (e < recheck_cap(cap)) RC[1 + e] = make_int2(i, j);
                     }
+                    oa = overlap_area<DIM>(r1, r2, r1sq, r2sq, m, rs, m < rm);
                     gf = oa * (q.inv - a.inv);
                     sAo += oa;
                     sAor = fmaf(oa, a.inv + q.inv, sAor);
@@ -380,8 +490,17 @@ __device__ __forceinline__ void k_pairs_mx_body(const Bufs &b, const int vb, con
         b.part[3 * vg + vb] = tAor;
     }
     if (last_block(&b.ctrl->done[DC_PAIRS], vg)) {
-        const double fAo = fold_partials(b.part + 2 * vg, vg, false, smem);
-        const double fAor = fold_partials(b.part + 3 * vg, vg, false, smem);
+        double fAo = fold_partials(b.part + 2 * vg, vg, false, smem);
+        double fAor = fold_partials(b.part + 3 * vg, vg, false, smem);
+        if (GAS) {
+            int2 *RC = recheck_list(AV, cap);
+            const float2 d = recheck_containment<DIM>(RC, b.ds, c, b.k, PB, AV, AO);
+            const double tdo = block_sum_f(d.x, smem);
+            const double tdor = block_sum_f(d.y, smem);
+            fAo += tdo;
+            fAor += tdor;
+            if (threadIdx.x == 0) RC[0].x = 0;  // every thread has read the count
+        }
         if (threadIdx.x == 0) {
             Ctrl *cc = b.ctrl;
             cc->sumAo = 2.0 * fAo;
@@ -393,7 +512,7 @@ __device__ __forceinline__ void k_pairs_mx_body(const Bufs &b, const int vb, con
         }
     }
 }
-CB_KERNEL_PAIR((template <int DIM, bool GAS, bool FLOW>), k_pairs_mx, (<DIM, GAS, FLOW>), __launch_bounds__(kBlock))
+CB_KERNEL_PAIR((template <int DIM, bool GAS, bool FLOW>), k_pairs_mx, (<DIM, GAS, FLOW>), __launch_bounds__(kBlock, 4))
 
 
 // ---------------------------------------------------------------- correct

@@ -133,3 +133,39 @@ def test_mixed_search_is_exact(oracle_mod):
     for k in ("x", "y", "z", "r", "saved_x"):
         assert np.array_equal(sg[k], so[k]), k
     assert np.array_equal(sg["index"], so["index"])
+
+
+@pytest.mark.parametrize("dim", [3, 2])
+def test_mixed_containment_threshold(oracle_mod, dim):
+    """A pair on the threshold where the overlap area jumps (one centre just
+    inside the other bubble, src/kernels.cu:240-249): the centres are
+    1 - 2^-30 apart and the larger radius is 1, so FP64 takes the containment
+    branch while the FP32 distance rounds to exactly 1 (the lens branch, an
+    area 6 % smaller in 3D). The mixed form decides such pairs again in FP64
+    and matches the oracle."""
+    d = 1.0 - 2.0 ** -30
+    L = 40.0
+    x = np.array([10.0, 10.0 + d, 25.0])
+    y = np.array([10.0, 10.0, 25.0])
+    z = np.array([10.0, 10.0, 25.0]) if dim == 3 else np.zeros(3)
+    r = np.array([1.0, 0.5, 0.8])
+    st = {"x": x, "y": y, "z": z, "r": r, "index": np.arange(3, dtype=np.int32)}
+    kw = dict(dimensionality=dim, lbb=(0.0, 0.0, 0.0), tfr=(L, L, L if dim == 3 else 0.0),
+              min_rad=0.1, f0_per_mu0=1.0, k_parameter=0.1, kappa=0.01, skin_radius=0.3,
+              bubble_volume_multiplier=1.0, average_surface_area_in=4.0,
+              error_tolerance=1e-5, time_step=1e-6, capacity=3)
+    o = oracle_mod.OracleFoam(cb.make_config(**kw))
+    g = cb.GpuFoam(cb.make_config(precision=1, **kw))
+    for f in (o, g):
+        f.load_state(st)
+        f.search_neighbors()
+    assert len(o.pairs()[0]) == 1
+    ag, ao = g.attempt(), o.attempt()
+    sg, so = g.get_state(), o.get_state()
+    og, oo = np.argsort(sg["index"]), np.argsort(so["index"])
+    # the containment branch: pi min(r)^2 (3D), 2 min(r) (2D)
+    expect = 0.25 * 3.1415926535897932 if dim == 3 else 1.0
+    assert ao["overlap"][oo][0] == pytest.approx(expect, rel=1e-12)
+    for k in ("overlap", "drdtp", "dxdtp"):
+        assert max_rel(ag[k][og], ao[k][oo]) <= 1e-6, k
+    assert ag["total_overlap_area"] == pytest.approx(ao["total_overlap_area"], rel=1e-6)
