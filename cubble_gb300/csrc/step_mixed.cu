@@ -286,13 +286,20 @@ __device__ __forceinline__ void pair_diff(const PredMx &a, const PredMx &q, cons
 
 // Overlap area of an overlapping pair (src/kernels.cu:236-256): min(r1, r2)^2
 // (3D, times pi) or 2 min(r1, r2) (2D) when one centre lies inside the other
-// bubble, else the lens formula.
+// bubble, else from the squared half chord a^2. The reference evaluates
+// a^2 = r2^2 - (r2^2 - r1^2 + d^2)^2 / (4 d^2), which cancels badly when a
+// small bubble sits on a large one (1.69 - 1.68 for radii 0.1 and 1.3); the
+// same quantity is evaluated here in the product form of the height of the
+// triangle (r1, r2, d), a^2 = ((r1 + r2)^2 - d^2) (d^2 - (r1 - r2)^2) / (4 d^2),
+// whose two factors carry the FP32 rounding of d^2 and the radii only.
 template <int DIM>
 __device__ __forceinline__ float overlap_area(float r1, float r2, float r1sq, float r2sq,
-                                              float m, float rs, bool inside) {
+                                              float radii, float m, float rs, bool inside) {
     if (inside) return DIM == 3 ? fminf(r1sq, r2sq) * (float)kPi : 2.f * fminf(r1, r2);
-    const float tt = 0.5f * (r2sq - r1sq + m);
-    const float oa = fabsf(r2sq - (tt * tt) * (rs * rs));
+    const float rd = r1 - r2;
+    const float p = fmaf(radii, radii, -m);
+    const float q = fmaf(-rd, rd, m);
+    const float oa = fabsf(p * q * (0.25f * (rs * rs)));
     return DIM == 3 ? oa * (float)kPi : 2.f * sqrtf(oa);
 }
 
@@ -344,9 +351,9 @@ __device__ __forceinline__ float2 recheck_containment(const int2 *RC, double *co
         const bool fast = m < fmaxf(r1sq, r2sq);
         const bool exact = contained_exact(ex, ey, ez, pr.x, pr.y, ds, c);
         if (fast == exact) continue;
-        const float rs = rsqrtf(m);
-        const float d = overlap_area<DIM>(r1, r2, r1sq, r2sq, m, rs, exact) -
-                        overlap_area<DIM>(r1, r2, r1sq, r2sq, m, rs, fast);
+        const float rs = rsqrtf(m), radii = r1 + r2;
+        const float d = overlap_area<DIM>(r1, r2, r1sq, r2sq, radii, m, rs, exact) -
+                        overlap_area<DIM>(r1, r2, r1sq, r2sq, radii, m, rs, fast);
         const float dg = d * (q.inv - a.inv);
         if (DIM == 3) {
             atomicAdd(AO + pr.x, d);
@@ -457,7 +464,7 @@ __device__ __forceinline__ void k_pairs_mx_body(const Bufs &b, const int vb, con
                         const int e = atomicAdd(&RC[0].x, 1);
                         if (e < recheck_cap(cap)) RC[1 + e] = make_int2(i, j);
                     }
-                    oa = overlap_area<DIM>(r1, r2, r1sq, r2sq, m, rs, m < rm);
+                    oa = overlap_area<DIM>(r1, r2, r1sq, r2sq, radii, m, rs, m < rm);
                     gf = oa * (q.inv - a.inv);
                     sAo += oa;
                     sAor = fmaf(oa, a.inv + q.inv, sAor);
@@ -612,7 +619,11 @@ __device__ __forceinline__ void k_correct_mx_body(const Bufs &b, const int vb, c
     float *AO = acc_ov(b, cap);
     float4 *AF = acc_fl(b, cap);
     // mean-field factors, src/kernels.cu:399-408 (computed once per attempt)
-    const float mfa = float_from_double(c->mfa), mfb = float_from_double(c->mfb);
+    // mfa (the area-weighted mean of 1/r) as float-float: mfa - 1/r is a
+    // difference of nearly equal terms, and one rounding of mfa would shift
+    // every bubble's gas flux the same way; mfb only scales the term
+    const ff mfa = ff_of(c->mfa);
+    const float mfb = float_from_double(c->mfb);
     const float kq = k.kq_f;
     const long long minr = __double_as_longlong(k.min_rad);
     const bool shear = c->use_flow && k.shear_on;
@@ -720,7 +731,7 @@ __device__ __forceinline__ void k_correct_mx_body(const Bufs &b, const int vb, c
         if (GAS) {  // mean-field gas exchange, src/kernels.cu:390-431
             const float inv = 1.f / rp;
             const float area = DIM == 3 ? (4.f * (float)kPi) * (rp * rp) : (2.f * (float)kPi) * rp;
-            float w = (mfa - inv) * (mfb * (area - ovl)) + vpr;
+            float w = ((mfa.h - inv) + mfa.l) * (mfb * (area - ovl)) + vpr;
             w *= DIM == 3 ? kq * (inv * inv) : kq * inv;
             vpr = w;
             const float ir = h * (vr + w);
