@@ -365,7 +365,7 @@ int cb_batch_create(const cb_config *cfgs, int32_t count, cb_batch **out) {
     };
     for (int f = 0; f < count; f++) {
         cb_context *c = nullptr;
-        int rc = cb_create(cfgs + f, &c);
+        int rc = cbg::create_context(cfgs + f, &c, false);
         if (rc) return bail(rc);
         b->foams.push_back(c);
     }
@@ -445,15 +445,26 @@ int cb_batch_set_tile(cb_batch *b, int32_t tile) {
     return CB_OK;
 }
 
+int cb_batch_set_tuning(cb_batch *b, const cb_tuning *t) {
+    if (!b || !t) return fail(CB_ERR_INVALID_ARGUMENT, "null argument");
+    for (cb_context *c : b->foams) {
+        CB_CUDA(cudaSetDevice(c->dev));
+        int rc = cbg::apply_tuning(c, *t);
+        if (rc) return rc;
+    }
+    if (b->gexec) {  // the batched graph holds the old launches
+        cudaGraphExecDestroy(b->gexec);
+        b->gexec = nullptr;
+    }
+    return CB_OK;
+}
+
 int cb_batch_autotune(cb_batch *b, int32_t steps, int32_t *tile_out) {
     if (!b || !tile_out) return fail(CB_ERR_INVALID_ARGUMENT, "null argument");
     if (steps < 1) return fail(CB_ERR_INVALID_ARGUMENT, "steps must be positive");
-    static const int kCand[] = {512, 1024, 2048, 4096, 8192};
     std::vector<cb_report> r0(b->foams.size()), r1(b->foams.size());
-    double best = -1.0;
-    int best_tile = b->tile;
-    for (int t : kCand) {
-        b->tile = t;
+    // bubble-steps per ms of `steps` steps with the current settings
+    auto trial = [&](double *rate) -> int {
         for (size_t f = 0; f < b->foams.size(); f++) {
             int rc = cb_get_report(b->foams[f], &r0[f]);
             if (rc) return rc;
@@ -463,13 +474,53 @@ int cb_batch_autotune(cb_batch *b, int32_t steps, int32_t *tile_out) {
         if (rc) return rc;
         long long bs = 0;
         for (size_t f = 0; f < b->foams.size(); f++) bs += r1[f].bubble_steps - r0[f].bubble_steps;
-        const double rate = ms > 0.0 ? (double)bs / ms : 0.0;
+        *rate = ms > 0.0 ? (double)bs / ms : 0.0;
+        return CB_OK;
+    };
+    double best = -1.0, rate = 0.0;
+    int best_tile = b->tile;
+    for (int t : {512, 1024, 2048, 4096, 8192}) {
+        b->tile = t;
+        int rc = trial(&rate);
+        if (rc) return rc;
         if (rate > best) {
             best = rate;
             best_tile = t;
         }
     }
     b->tile = best_tile;
+    // the cell edge, then the mixed pair kernel's pairs per thread
+    cb_tuning bt = b->first()->tune;
+    const cb_tuning keep0 = bt;
+    best = -1.0;
+    for (double cs : {1.0, 1.15, 1.3}) {
+        cb_tuning q = keep0;
+        q.cell_scale = cs;
+        int rc = cb_batch_set_tuning(b, &q);
+        if (!rc) rc = trial(&rate);
+        if (rc) return rc;
+        if (rate > best) {
+            best = rate;
+            bt = q;
+        }
+    }
+    if (b->first()->hk.mixed) {
+        const cb_tuning keep1 = bt;
+        best = -1.0;
+        for (int run : {2, 4, 8}) {
+            cb_tuning q = keep1;
+            q.pair_run = run;
+            int rc = cb_batch_set_tuning(b, &q);
+            if (!rc) rc = trial(&rate);
+            if (rc) return rc;
+            if (rate > best) {
+                best = rate;
+                bt = q;
+            }
+        }
+    }
+    int rc = cb_batch_set_tuning(b, &bt);
+    if (rc) return rc;
     *tile_out = best_tile;
     return CB_OK;
 }

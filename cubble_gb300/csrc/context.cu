@@ -5,6 +5,8 @@
 // conditional nodes are driven by the device (no host round trip per step).
 #include <algorithm>
 #include <cmath>
+#include <map>
+#include <mutex>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -98,6 +100,32 @@ void fill_const(cb_context *c) {
     k.shear_il = k.iv[k.shear_axis] > 0.0 ? 2.0 / k.iv[k.shear_axis] : 0.0;
     k.shear_f = (float)k.shear;
     k.shear_il_f = (float)k.shear_il;
+    k.cell_scale = c->tune.cell_scale >= 1.0 ? c->tune.cell_scale : 1.0;
+}
+
+// Process-wide choices of cb_autotune, by dimensionality, precision and
+// capacity bucket floor(log2(capacity)).
+std::mutex g_tune_mu;
+std::map<long long, cb_tuning> g_tune_cache;
+
+long long tune_key(const cb_config &f) {
+    int b = 0;
+    while (b < 31 && (1LL << (b + 1)) <= (long long)f.capacity) b++;
+    return (long long)f.dimensionality * 1000 + (long long)f.precision * 100 + b;
+}
+
+// Largest radius of a row into ctrl->max_bubble_radius, which the caller
+// zeroed: positive finite doubles order as their bit patterns do.
+__global__ void __launch_bounds__(kBlock) k_max_radius(const double *R, int n, Ctrl *ctrl) {
+    long long m = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const long long v = __double_as_longlong(R[i]);
+        if (v < 0x7ff0000000000000LL) m = max(m, v);  // finite and positive radii only
+    }
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m > 0)
+        atomicMax(reinterpret_cast<unsigned long long *>(&ctrl->max_bubble_radius),
+                  (unsigned long long)m);
 }
 
 }  // namespace
@@ -328,6 +356,16 @@ extern "C" {
 const char *cb_last_error(void) { return g_err.c_str(); }
 
 int cb_create(const cb_config *cfg, cb_context **out) {
+    return cbg::create_context(cfg, out, true);
+}
+
+}  // extern "C"
+
+// cb_create; with `graph` and cfg->use_graph the integrate() graph of the
+// context's options is built and instantiated here, so that the first
+// cb_integrate does not pay for it (the foams of a batch skip it: the batch
+// runs its own graph).
+int cbg::create_context(const cb_config *cfg, cb_context **out, bool graph) {
     if (!cfg || !out) return fail(CB_ERR_INVALID_ARGUMENT, "null argument");
     *out = nullptr;
     if (cfg->dimensionality != 2 && cfg->dimensionality != 3)
@@ -441,11 +479,25 @@ int cb_create(const cb_config *cfg, cb_context **out) {
     h.use_gas = cfg->use_gas_exchange ? 1 : 0;
     h.use_flow = cfg->use_flow ? 1 : 0;
     h.inc_path = cfg->increment_path ? 1 : 0;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        auto it = g_tune_cache.find(tune_key(*cfg));
+        if (it != g_tune_cache.end()) {
+            c->tune = it->second;
+            c->launch.pair_run = c->tune.pair_run;
+            c->launch.pair_bps = c->tune.pair_blocks;
+            c->launch.step_bps = c->tune.step_blocks;
+            fill_const(c);
+        }
+    }
     if ((rc = c->upload_const())) return bail(rc);
     if ((rc = c->push())) return bail(rc);
+    if (graph && cfg->use_graph && (rc = build_graph(c))) return bail(rc);
     *out = c;
     return CB_OK;
 }
+
+extern "C" {
 
 int cb_destroy(cb_context *c) {
     if (!c) return CB_OK;
@@ -530,17 +582,23 @@ int cb_load_state(cb_context *c, const cb_state_view *s) {
             CB_CUDA(cudaMemsetAsync(dst, 0, (size_t)c->hk.cap * 4, c->stream));
     }
     CB_CUDA(cudaMemsetAsync(c->bufs.acc, 0, (size_t)kAcc * c->hk.cap * 8, c->stream));
-    double mr = 0.0;
-    for (size_t i = 0; i < n; i++) mr = std::max(mr, s->r[i]);
     h.n = s->count;
     h.np = 0;
     h.ndel = 0;
     h.status = CB_OK;
-    h.max_bubble_radius = mr;
+    h.max_bubble_radius = 0.0;
     h.too_large = h.need_search = h.need_delete = h.attempts_this_step = 0;
     h.pred_ready = 0;
     h.pred_slot = 0;
-    rc = c->push();  // synchronises, so the caller's buffers are free
+    CB_CUDA(cudaMemcpyAsync(c->dctrl, c->hctrl, sizeof(Ctrl), cudaMemcpyHostToDevice, c->stream));
+    // the largest radius (HostData.maxBubbleRadius) from the uploaded row
+    if (n) {
+        k_max_radius<<<std::min<int>(c->launch.grid, (int)((n + kBlock - 1) / kBlock)), kBlock, 0,
+                       c->stream>>>(c->dslot[h.drole[RR]], (int)n, c->dctrl);
+        c->launches += 1;
+        if ((rc = c->check_launch())) return rc;
+    }
+    rc = c->pull();  // synchronises, so the caller's buffers are free
     if (rc) return rc;
     c->loaded = true;
     return CB_OK;
@@ -920,10 +978,13 @@ int cb_total_volume(cb_context *c, double *out) {
     return CB_OK;
 }
 
-int cb_profile_kernels(cb_context *c, int32_t reps, double ms[3]) {
-    CB_ENTER(c);
-    if (!c->loaded) return fail(CB_ERR_STATE, "state not loaded");
-    if (reps < 1 || !ms) return fail(CB_ERR_INVALID_ARGUMENT, "bad arguments");
+}  // extern "C"
+
+namespace {
+
+// Mean device ms of predict, pairs and correct over `reps` attempts that are
+// not accepted; the control block (dt, counters) is restored afterwards.
+int profile_attempts(cb_context *c, int32_t reps, double ms[3]) {
     int rc = c->pull();
     if (rc) return rc;
     Ctrl saved = *c->hctrl;
@@ -932,7 +993,6 @@ int cb_profile_kernels(cb_context *c, int32_t reps, double ms[3]) {
     cudaEvent_t ev[4];
     for (int q = 0; q < 4; q++) CB_CUDA(cudaEventCreate(&ev[q]));
     double acc[3] = {0, 0, 0};
-    const int dim = c->hk.dim;
     // one attempt untimed: the first launch of a kernel also loads its code
     launch_attempt_kernels(c, c->launch, c->bufs);
     CB_CUDA(cudaStreamSynchronize(c->stream));
@@ -955,22 +1015,18 @@ int cb_profile_kernels(cb_context *c, int32_t reps, double ms[3]) {
     for (int q = 0; q < 3; q++) ms[q] = acc[q] / reps;
     if ((rc = c->check_launch())) return rc;
     if ((rc = c->pull())) return rc;
-    // restore the control block (dt, counters) as before the measurement
     const int status = c->hctrl->status;
     *c->hctrl = saved;
     c->hctrl->status = status;
     return c->push();
 }
 
-int cb_profile_search(cb_context *c, int32_t reps, double *ms) {
-    NvtxRange nv("Neighbors");
-    CB_ENTER(c);
-    if (!c->loaded) return fail(CB_ERR_STATE, "state not loaded");
-    if (reps < 1 || !ms) return fail(CB_ERR_INVALID_ARGUMENT, "bad arguments");
+// Mean device ms of one search over `reps` searches of the current state
+// (after one untimed search); the search counter is restored.
+int profile_searches(cb_context *c, int32_t reps, double *ms) {
     int rc = c->pull();
     if (rc) return rc;
     const long long searches0 = c->hctrl->searches;
-    // one search untimed: the first launch of a kernel also loads its code
     if ((rc = run_search(c))) return rc;
     CB_CUDA(cudaStreamSynchronize(c->stream));
     CB_CUDA(cudaEventRecord(c->ev0, c->stream));
@@ -984,6 +1040,131 @@ int cb_profile_search(cb_context *c, int32_t reps, double *ms) {
     if ((rc = sync_status(c))) return rc;
     c->hctrl->searches = searches0;  // measurement searches are not the run's
     return c->push();
+}
+
+}  // namespace
+
+// Validates and applies a tuning: the launch knobs, the cell scale of the
+// device constants, and a rebuild of the integrate graph at its next use.
+int cbg::apply_tuning(cb_context *c, const cb_tuning &t) {
+    if (!(t.cell_scale >= 1.0 && t.cell_scale <= 4.0))
+        return fail(CB_ERR_INVALID_ARGUMENT, "cell_scale must lie in [1, 4]");
+    if (t.pair_run != 0 && t.pair_run != 2 && t.pair_run != 4 && t.pair_run != 8)
+        return fail(CB_ERR_INVALID_ARGUMENT, "pair_run must be 0, 2, 4 or 8");
+    if (t.pair_blocks < 0 || t.pair_blocks > 8 || t.step_blocks < 0 || t.step_blocks > 8)
+        return fail(CB_ERR_INVALID_ARGUMENT, "blocks per SM must lie in 0 ... 8");
+    c->tune = t;
+    if (c->tune.pair_run == 0) c->tune.pair_run = 4;
+    c->launch.pair_run = c->tune.pair_run;
+    c->launch.pair_bps = c->tune.pair_blocks;
+    c->launch.step_bps = c->tune.step_blocks;
+    fill_const(c);
+    if (c->gexec) {
+        cudaGraphExecDestroy(c->gexec);
+        c->gexec = nullptr;
+    }
+    c->graph_key = -1;
+    return c->upload_const();
+}
+
+extern "C" {
+
+int cb_profile_kernels(cb_context *c, int32_t reps, double ms[3]) {
+    CB_ENTER(c);
+    if (!c->loaded) return fail(CB_ERR_STATE, "state not loaded");
+    if (reps < 1 || !ms) return fail(CB_ERR_INVALID_ARGUMENT, "bad arguments");
+    return profile_attempts(c, reps, ms);
+}
+
+int cb_profile_search(cb_context *c, int32_t reps, double *ms) {
+    NvtxRange nv("Neighbors");
+    CB_ENTER(c);
+    if (!c->loaded) return fail(CB_ERR_STATE, "state not loaded");
+    if (reps < 1 || !ms) return fail(CB_ERR_INVALID_ARGUMENT, "bad arguments");
+    return profile_searches(c, reps, ms);
+}
+
+int cb_set_tuning(cb_context *c, const cb_tuning *t) {
+    CB_ENTER(c);
+    if (!t) return fail(CB_ERR_INVALID_ARGUMENT, "null tuning");
+    return apply_tuning(c, *t);
+}
+
+int cb_forget_tuning(void) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune_cache.clear();
+    return CB_OK;
+}
+
+int cb_get_tuning(cb_context *c, cb_tuning *t) {
+    if (!c || !t) return fail(CB_ERR_INVALID_ARGUMENT, "null argument");
+    *t = c->tune;
+    return CB_OK;
+}
+
+int cb_autotune(cb_context *c, int32_t reps, cb_tuning *best) {
+    CB_ENTER(c);
+    if (!c->loaded) return fail(CB_ERR_STATE, "state not loaded");
+    if (reps < 1 || !best) return fail(CB_ERR_INVALID_ARGUMENT, "bad arguments");
+    int rc = c->pull();
+    if (rc) return rc;
+    if (c->hctrl->np < 1) return fail(CB_ERR_STATE, "no pair list: search first");
+    cb_tuning t = c->tune;
+    double ms[3];
+    // pair kernel: pairs per thread x resident blocks per SM
+    const int runs_mx[] = {2, 4, 8}, runs_one[] = {4};
+    const int *runs = c->hk.mixed ? runs_mx : runs_one;
+    const int nruns = c->hk.mixed ? 3 : 1;
+    const int blocks[] = {0, 2, 3};
+    double best_pairs = 1e300;
+    cb_tuning bt = t;
+    for (int r = 0; r < nruns; r++)
+        for (int bl : blocks) {
+            cb_tuning q = t;
+            q.pair_run = runs[r];
+            q.pair_blocks = bl;
+            if ((rc = apply_tuning(c, q)) || (rc = profile_attempts(c, reps, ms))) return rc;
+            if (ms[1] < best_pairs) {
+                best_pairs = ms[1];
+                bt.pair_run = q.pair_run;
+                bt.pair_blocks = q.pair_blocks;
+            }
+        }
+    // predict + correct: resident blocks per SM
+    double best_step = 1e300;
+    for (int bl : {0, 1, 2, 3}) {
+        cb_tuning q = bt;
+        q.step_blocks = bl;
+        if ((rc = apply_tuning(c, q)) || (rc = profile_attempts(c, reps, ms))) return rc;
+        if (ms[0] + ms[2] < best_step) {
+            best_step = ms[0] + ms[2];
+            bt.step_blocks = bl;
+        }
+    }
+    // neighbour search: cell edge
+    double best_search = 1e300;
+    for (double cs : {1.0, 1.15, 1.3, 1.5}) {
+        cb_tuning q = bt;
+        q.cell_scale = cs;
+        double sm = 0.0;
+        if ((rc = apply_tuning(c, q)) || (rc = profile_searches(c, reps, &sm))) return rc;
+        if (sm < best_search) {
+            best_search = sm;
+            bt.cell_scale = cs;
+        }
+    }
+    if ((rc = apply_tuning(c, bt))) return rc;
+    // leave the state searched with the chosen cells
+    if ((rc = run_search(c)) || (rc = sync_status(c))) return rc;
+    if ((rc = c->pull())) return rc;
+    c->hctrl->searches -= 1;  // a measurement search, not the run's
+    if ((rc = c->push())) return rc;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_tune_cache[tune_key(c->cfg)] = bt;
+    }
+    *best = bt;
+    return CB_OK;
 }
 
 int cb_launch_count(cb_context *c, int64_t *count) {

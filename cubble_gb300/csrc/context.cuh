@@ -62,6 +62,8 @@ struct cb_context {
     // device's control block and the stream idle
     unsigned long long mirror_call = ~0ull;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // launch / search knobs (cb_tuning); their launch parts live in `launch`
+    cb_tuning tune{1.0, 4, 0, 0, 0};
 
     template <typename T>
     int alloc(T **p, size_t n) {
@@ -115,4 +117,6 @@ int capture_conditional(cudaStream_t stream, cudaGraphConditionalNodeType type,
                         cudaGraphConditionalHandle *handle, unsigned int dflt,
                         cudaGraph_t *body);
 void fill_report(const cb_context *c, cb_report *r);
+int create_context(const cb_config *cfg, cb_context **out, bool graph);
+int apply_tuning(cb_context *c, const cb_tuning &t);
 }  // namespace cbg
