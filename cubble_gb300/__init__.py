@@ -71,6 +71,22 @@ class GpuFoam(Foam):
         self._call("launch_count", self._ctx, C.byref(n))
         return n.value
 
+    def set_tuning(self, cell_scale=1.0, pair_run=4, pair_blocks=0, step_blocks=0):
+        t = _abi.Tuning(float(cell_scale), int(pair_run), int(pair_blocks), int(step_blocks), 0)
+        self._call("set_tuning", self._ctx, C.byref(t))
+
+    def tuning(self):
+        t = _abi.Tuning()
+        self._call("get_tuning", self._ctx, C.byref(t))
+        return t.as_dict()
+
+    def autotune(self, reps=3):
+        """Times the knobs of cb_tuning on the current (searched) state, keeps
+        the fastest (also for later contexts of the same kind), returns them."""
+        t = _abi.Tuning()
+        self._call("autotune", self._ctx, int(reps), C.byref(t))
+        return t.as_dict()
+
     def integrate_until(self, max_steps, time=None, min_count=-1, max_radius=float("inf")):
         """Up to max_steps accepted steps, ending after the first one that
         reaches `time` (the simulation clock), leaves <= min_count bubbles
@@ -170,15 +186,16 @@ class GpuFoamBatch:
         self._call("batch_set_tile", self._b, int(bubbles_per_block))
 
     def autotune(self, steps_per_trial):
+        """Tile, cell scale and (mixed form) pairs per thread, each timed over
+        `steps_per_trial` steps that advance the foams; returns the tile (the
+        other knobs: foams[0].tuning())."""
         t = C.c_int32()
         self._call("batch_autotune", self._b, int(steps_per_trial), C.byref(t))
         return t.value
 
-    def profile_search(self, reps=3):
-        """Mean device ms of one neighbour search of the current state."""
-        ms = C.c_double()
-        self._call("profile_search", self._ctx, int(reps), C.byref(ms))
-        return ms.value
+    def set_tuning(self, cell_scale=1.0, pair_run=4, pair_blocks=0, step_blocks=0):
+        t = _abi.Tuning(float(cell_scale), int(pair_run), int(pair_blocks), int(step_blocks), 0)
+        self._call("batch_set_tuning", self._b, C.byref(t))
 
     def launch_count(self):
         n = C.c_int64()

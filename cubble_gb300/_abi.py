@@ -121,6 +121,15 @@ class AttemptView(C.Structure):
                 + [("num_to_be_deleted", C.c_int32), ("pad_", C.c_int32)])
 
 
+class Tuning(C.Structure):
+    """cb_tuning: launch and search knobs of a context."""
+    _fields_ = [("cell_scale", C.c_double), ("pair_run", C.c_int32),
+                ("pair_blocks", C.c_int32), ("step_blocks", C.c_int32), ("pad_", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad_"}
+
+
 def declare(lib, prefix):
     """Declares the prototypes of include/cubble_gb300.h on `lib` for the
     given symbol prefix ("cb_" for the CUDA library)."""
@@ -152,6 +161,11 @@ def declare(lib, prefix):
             "launch_count": (C.c_int, [vp, C.POINTER(C.c_int64)]),
             "profile_kernels": (C.c_int, [vp, C.c_int32, C.POINTER(C.c_double)]),
             "profile_search": (C.c_int, [vp, C.c_int32, C.POINTER(C.c_double)]),
+            "set_tuning": (C.c_int, [vp, C.POINTER(Tuning)]),
+            "get_tuning": (C.c_int, [vp, C.POINTER(Tuning)]),
+            "autotune": (C.c_int, [vp, C.c_int32, C.POINTER(Tuning)]),
+            "forget_tuning": (C.c_int, []),
+            "batch_set_tuning": (C.c_int, [vp, C.POINTER(Tuning)]),
             "energy_noalloc": (C.c_int, [C.POINTER(Config), vp, vp, vp, vp, vp, vp,
                                          C.c_int32, C.c_int32, vp, vp]),
             "integrate_until": (C.c_int, [vp, C.c_int64, C.POINTER(Stop), C.POINTER(Report)]),

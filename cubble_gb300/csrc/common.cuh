@@ -89,6 +89,9 @@ struct DevConst {
     int shear_on, shear_axis;
     double shear, shear_il;
     float shear_f, shear_il_f;
+    // Cell edge of the neighbour search in units of 2 maxR + skin (>= 1; a
+    // tuning knob, cb_tuning.cell_scale)
+    double cell_scale;
 };
 
 // Device control block. The host reads it after each eager phase or at the
@@ -576,6 +579,12 @@ struct Launch {
     const struct Bufs *batch = nullptr;
     const struct BatchWork *work = nullptr;
     int gmax = 0;
+    // Tuning (cb_tuning): consecutive pairs per thread of the mixed pair
+    // kernel, and resident blocks per SM of the pair kernels and of the
+    // predict / correct kernels (0: as many as fit)
+    int pair_run = 4;
+    int pair_bps = 0;
+    int step_bps = 0;
 };
 
 // Phases of a batched step a foam takes part in (Ctrl::bsel bits).
@@ -667,12 +676,14 @@ inline void launch_pdl(void (*kernel)(KArgs...), int grid, cudaStream_t stream, 
 
 // One wave of resident blocks of `kernel` (a multiple of the SM count),
 // bounded by l.grid (the size of the per-block partial arrays).
+// `want` > 0 caps the resident blocks per SM (a tuning knob).
 template <typename K>
-inline int wave_grid(K kernel, const Launch &l) {
+inline int wave_grid(K kernel, const Launch &l, int want = 0) {
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kBlock, 0) != cudaSuccess ||
         nb < 1)
         nb = 1;
+    if (want > 0 && want < nb) nb = want;
     const int g = l.sms * nb;
     return g < l.grid ? g : l.grid;
 }

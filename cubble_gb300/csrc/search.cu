@@ -25,11 +25,13 @@
 namespace cbg {
 namespace {
 
-// Cell grid: cellDim_a = max(1, floor(interval_a / (2 maxR + skin))) on the
-// used axes; while the product exceeds the cell capacity the largest
-// dimension (lowest axis on ties) shrinks by one.
+// Cell grid: cellDim_a = max(1, floor(interval_a / (s (2 maxR + skin)))) on
+// the used axes, s = k.cell_scale >= 1 (1 by default); while the product
+// exceeds the cell capacity the largest dimension (lowest axis on ties)
+// shrinks by one. Larger cells change which candidates are tested and the
+// bubble order, never the pair set.
 __device__ void cell_grid(const DevConst &k, double max_r, int cd[3]) {
-    const double cutoff = __dadd_rn(__dmul_rn(2.0, max_r), k.skin);
+    const double cutoff = __dmul_rn(__dadd_rn(__dmul_rn(2.0, max_r), k.skin), k.cell_scale);
     for (int a = 0; a < 3; a++) {
         cd[a] = 1;
         if (a < k.dim) {

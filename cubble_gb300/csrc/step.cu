@@ -915,9 +915,9 @@ __global__ void __launch_bounds__(kBlock) k_volume(Bufs b) {
 
 void launch_predict(const Launch &l, const Bufs &b, int dim) {
     if (dim == 3)
-        CB_LAUNCH(l, k_predict, (<3>), wave_grid(k_predict<3>, l), b);
+        CB_LAUNCH(l, k_predict, (<3>), wave_grid(k_predict<3>, l, l.step_bps), b);
     else
-        CB_LAUNCH(l, k_predict, (<2>), wave_grid(k_predict<2>, l), b);
+        CB_LAUNCH(l, k_predict, (<2>), wave_grid(k_predict<2>, l, l.step_bps), b);
 }
 
 // mode bits: 1 = gas exchange, 2 = flow. mode 0 is the bootstrap form.
@@ -926,9 +926,9 @@ void launch_pairs(const Launch &l, const Bufs &b, int dim, int mode, bool ff) {
 #define CB_PAIRS(D, G, F)                                                                     \
     do {                                                                                      \
         if (ff)                                                                               \
-            CB_LAUNCH(l, k_pairs_ff, (<D, G, F>), wave_grid(k_pairs_ff<D, G, F>, l), b);      \
+            CB_LAUNCH(l, k_pairs_ff, (<D, G, F>), wave_grid(k_pairs_ff<D, G, F>, l, l.pair_bps), b);      \
         else                                                                                  \
-            CB_LAUNCH(l, k_pairs, (<D, G, F>), wave_grid(k_pairs<D, G, F>, l), b);            \
+            CB_LAUNCH(l, k_pairs, (<D, G, F>), wave_grid(k_pairs<D, G, F>, l, l.pair_bps), b);            \
     } while (0)
     if (dim == 3) {
         if (gas && flow) CB_PAIRS(3, true, true);
@@ -946,9 +946,9 @@ void launch_pairs(const Launch &l, const Bufs &b, int dim, int mode, bool ff) {
 
 void launch_correct(const Launch &l, const Bufs &b, int dim) {
     if (dim == 3)
-        CB_LAUNCH(l, k_correct, (<3>), wave_grid(k_correct<3>, l), b);
+        CB_LAUNCH(l, k_correct, (<3>), wave_grid(k_correct<3>, l, l.step_bps), b);
     else
-        CB_LAUNCH(l, k_correct, (<2>), wave_grid(k_correct<2>, l), b);
+        CB_LAUNCH(l, k_correct, (<2>), wave_grid(k_correct<2>, l, l.step_bps), b);
 }
 
 void launch_boot(const Launch &l, const Bufs &b, int dim, int phase) {

@@ -370,15 +370,35 @@ __device__ __forceinline__ float2 recheck_containment(const int2 *RC, double *co
     return make_float2(so, sor);
 }
 
-// The search emits the pairs grouped by i in ascending order, so consecutive
-// pairs mostly share their first bubble. Each thread takes a run of kRun
-// consecutive pairs (one 16-byte load of the i's and one of the j's), loads
-// the prediction of i once per distinct i, keeps i's sums in registers and
-// adds them with one vector reduction per distinct i; the j side adds per
-// pair. In 2D the overlap sum rides in the third lane of the velocity float4.
-constexpr int kRun = 4;
+// RUN consecutive entries of a pair-list row with vector loads (the run
+// starts at a multiple of RUN, so the loads are aligned).
+template <int RUN>
+__device__ __forceinline__ void load_run(const int *P, int p0, int (&v)[RUN]) {
+    if (RUN == 2) {
+        const int2 u = *reinterpret_cast<const int2 *>(P + p0);
+        v[0] = u.x;
+        v[1] = u.y;
+    } else {
+#pragma unroll
+        for (int h = 0; h < RUN; h += 4) {
+            const int4 u = *reinterpret_cast<const int4 *>(P + p0 + h);
+            v[h] = u.x;
+            v[h + 1] = u.y;
+            v[h + 2] = u.z;
+            v[h + 3] = u.w;
+        }
+    }
+}
 
-template <int DIM, bool GAS, bool FLOW>
+// The search emits the pairs grouped by i in ascending order, so consecutive
+// pairs mostly share their first bubble. Each thread takes a run of RUN
+// consecutive pairs (vector loads of the i's and of the j's), loads the
+// prediction of i once per distinct i, keeps i's sums in registers and adds
+// them with one vector reduction per distinct i; the j side adds per pair.
+// In 2D the overlap sum rides in the third lane of the velocity float4. RUN
+// (pairs per thread, 32 RUN per warp) is a tuning knob: 4 by default, 2 or 8
+// for the gas-exchange kernels without flow (cb_tuning.pair_run).
+template <int DIM, bool GAS, bool FLOW, int RUN>
 __device__ __forceinline__ void k_pairs_mx_body(const Bufs &b, const int vb, const int vg) {
     __shared__ double smem[32];
     const Ctrl *c = b.ctrl;
@@ -395,18 +415,16 @@ __device__ __forceinline__ void k_pairs_mx_body(const Bufs &b, const int vb, con
     const FixBox fb = fix_box(k, DIM);
     const double *PB = pred_base(b, c, cap);
     float sAo = 0.f, sAor = 0.f;
-    const int nrun = (np + kRun - 1) / kRun;
+    const int nrun = (np + RUN - 1) / RUN;
     for (int g = vb * blockDim.x + threadIdx.x; g < nrun; g += vg * blockDim.x) {
-        const int p0 = g * kRun;
-        int I[kRun], J[kRun];
-        if (p0 + kRun <= np) {
-            const int4 u = *reinterpret_cast<const int4 *>(PI + p0);
-            const int4 v = *reinterpret_cast<const int4 *>(PJ + p0);
-            I[0] = u.x; I[1] = u.y; I[2] = u.z; I[3] = u.w;
-            J[0] = v.x; J[1] = v.y; J[2] = v.z; J[3] = v.w;
+        const int p0 = g * RUN;
+        int I[RUN], J[RUN];
+        if (p0 + RUN <= np) {
+            load_run<RUN>(PI, p0, I);
+            load_run<RUN>(PJ, p0, J);
         } else {
 #pragma unroll
-            for (int t = 0; t < kRun; t++) {
+            for (int t = 0; t < RUN; t++) {
                 I[t] = p0 + t < np ? PI[p0 + t] : -1;
                 J[t] = p0 + t < np ? PJ[p0 + t] : 0;
             }
@@ -426,7 +444,7 @@ __device__ __forceinline__ void k_pairs_mx_body(const Bufs &b, const int vb, con
             if (FLOW) red_add4(AF + cur, fx_i, fy_i, fz_i, 0.f);
         };
 #pragma unroll
-        for (int t = 0; t < kRun; t++) {
+        for (int t = 0; t < RUN; t++) {
             const int i = I[t], j = J[t];
             if (i < 0) break;
             if (i != cur) {
@@ -519,7 +537,7 @@ __device__ __forceinline__ void k_pairs_mx_body(const Bufs &b, const int vb, con
         }
     }
 }
-CB_KERNEL_PAIR((template <int DIM, bool GAS, bool FLOW>), k_pairs_mx, (<DIM, GAS, FLOW>), __launch_bounds__(kBlock, 4))
+CB_KERNEL_PAIR((template <int DIM, bool GAS, bool FLOW, int RUN>), k_pairs_mx, (<DIM, GAS, FLOW, RUN>), __launch_bounds__(kBlock, 4))
 
 
 // ---------------------------------------------------------------- correct
@@ -886,40 +904,46 @@ template <int DIM, bool GAS>
 void launch_correct_mx_t(const Launch &l, const Bufs &b, bool flow, bool walls) {
     if (flow && walls)
         CB_LAUNCH(l, k_correct_mx, (<DIM, GAS, true, true>),
-                  wave_grid(k_correct_mx<DIM, GAS, true, true>, l), b);
+                  wave_grid(k_correct_mx<DIM, GAS, true, true>, l, l.step_bps), b);
     else if (flow)
         CB_LAUNCH(l, k_correct_mx, (<DIM, GAS, true, false>),
-                  wave_grid(k_correct_mx<DIM, GAS, true, false>, l), b);
+                  wave_grid(k_correct_mx<DIM, GAS, true, false>, l, l.step_bps), b);
     else if (walls)
         CB_LAUNCH(l, k_correct_mx, (<DIM, GAS, false, true>),
-                  wave_grid(k_correct_mx<DIM, GAS, false, true>, l), b);
+                  wave_grid(k_correct_mx<DIM, GAS, false, true>, l, l.step_bps), b);
     else
         CB_LAUNCH(l, k_correct_mx, (<DIM, GAS, false, false>),
-                  wave_grid(k_correct_mx<DIM, GAS, false, false>, l), b);
+                  wave_grid(k_correct_mx<DIM, GAS, false, false>, l, l.step_bps), b);
 }
 
 }  // namespace
 
 void launch_predict_mx(const Launch &l, const Bufs &b, int dim) {
     if (dim == 3)
-        CB_LAUNCH(l, k_predict_mx, (<3>), wave_grid(k_predict_mx<3>, l), b);
+        CB_LAUNCH(l, k_predict_mx, (<3>), wave_grid(k_predict_mx<3>, l, l.step_bps), b);
     else
-        CB_LAUNCH(l, k_predict_mx, (<2>), wave_grid(k_predict_mx<2>, l), b);
+        CB_LAUNCH(l, k_predict_mx, (<2>), wave_grid(k_predict_mx<2>, l, l.step_bps), b);
 }
 
 void launch_pairs_mx(const Launch &l, const Bufs &b, int dim, int mode) {
     const bool gas = mode & 1, flow = mode & 2;
-#define CB_PAIRS(D, G, F) CB_LAUNCH(l, k_pairs_mx, (<D, G, F>), wave_grid(k_pairs_mx<D, G, F>, l), b)
+    const int run = l.pair_run;
+#define CB_PAIRS(D, G, F, R) \
+    CB_LAUNCH(l, k_pairs_mx, (<D, G, F, R>), wave_grid(k_pairs_mx<D, G, F, R>, l, l.pair_bps), b)
     if (dim == 3) {
-        if (gas && flow) CB_PAIRS(3, true, true);
-        else if (gas) CB_PAIRS(3, true, false);
-        else if (flow) CB_PAIRS(3, false, true);
-        else CB_PAIRS(3, false, false);
+        if (gas && flow) CB_PAIRS(3, true, true, 4);
+        else if (gas && run == 2) CB_PAIRS(3, true, false, 2);
+        else if (gas && run == 8) CB_PAIRS(3, true, false, 8);
+        else if (gas) CB_PAIRS(3, true, false, 4);
+        else if (flow) CB_PAIRS(3, false, true, 4);
+        else CB_PAIRS(3, false, false, 4);
     } else {
-        if (gas && flow) CB_PAIRS(2, true, true);
-        else if (gas) CB_PAIRS(2, true, false);
-        else if (flow) CB_PAIRS(2, false, true);
-        else CB_PAIRS(2, false, false);
+        if (gas && flow) CB_PAIRS(2, true, true, 4);
+        else if (gas && run == 2) CB_PAIRS(2, true, false, 2);
+        else if (gas && run == 8) CB_PAIRS(2, true, false, 8);
+        else if (gas) CB_PAIRS(2, true, false, 4);
+        else if (flow) CB_PAIRS(2, false, true, 4);
+        else CB_PAIRS(2, false, false, 4);
     }
 #undef CB_PAIRS
 }

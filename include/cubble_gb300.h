@@ -285,6 +285,43 @@ CB_API int cb_profile_kernels(cb_context *ctx, int32_t reps, double ms[3]);
  * searched; the report's search counter does not count these. */
 CB_API int cb_profile_search(cb_context *ctx, int32_t reps, double *ms);
 
+/* ------------------------------------------------------------- tuning
+ * Launch and search knobs of a context. None changes the pair set or the
+ * arithmetic of a pair; they change how work is cut into threads, blocks and
+ * cells (so the bubble order after a search and the order of reductions,
+ * which moves FP64 sums by rounding only). No counterpart in the reference,
+ * whose launch shape is fixed (5120 x 384, src/data_definitions.h:28-29) and
+ * whose cell edge is 2 (maxR + skin) (src/simulator.cu:69-75). */
+typedef struct cb_tuning {
+    double cell_scale;   /* cell edge of the neighbour search in units of
+                            2 maxR + skin, in [1, 4]; 1 = default          */
+    int32_t pair_run;    /* mixed form: consecutive pairs per thread of the
+                            pair kernel (2, 4 or 8; 32 x that per warp); 0 = 4 */
+    int32_t pair_blocks; /* resident blocks per SM of the pair kernel,
+                            0..8; 0 = as many as fit                       */
+    int32_t step_blocks; /* resident blocks per SM of the predict and correct
+                            kernels, 0..8; 0 = as many as fit              */
+    int32_t pad_;
+} cb_tuning;
+
+/* Sets / reads the knobs of a context (the next integrate rebuilds its
+ * graph). */
+CB_API int cb_set_tuning(cb_context *ctx, const cb_tuning *tuning);
+CB_API int cb_get_tuning(cb_context *ctx, cb_tuning *tuning);
+
+/* Autotuner: on the loaded, searched state, times the pair kernel for every
+ * (pair_run, pair_blocks) candidate and the predict + correct kernels for
+ * every step_blocks candidate (`reps` attempts each, not accepted: the state
+ * does not advance), and one neighbour search per cell_scale candidate (the
+ * state is left searched); keeps the fastest of each and returns them in
+ * *best. The choice is also kept process-wide for contexts of the same
+ * dimensionality, precision and capacity bucket (floor(log2(capacity))):
+ * cb_create applies it to every later context of that kind. */
+CB_API int cb_autotune(cb_context *ctx, int32_t reps, cb_tuning *best);
+/* Forgets every choice cb_autotune kept: later contexts start from the
+ * defaults (existing contexts keep their knobs). */
+CB_API int cb_forget_tuning(void);
+
 /* Number of kernels this library launched on the context so far (graph
  * kernel nodes are counted per execution). */
 CB_API int cb_launch_count(cb_context *ctx, int64_t *count);
@@ -319,9 +356,13 @@ CB_API int cb_batch_integrate_timed(cb_batch *batch, int64_t n_steps, cb_report 
  * >= 256); the default is 2048. */
 CB_API int cb_batch_set_tile(cb_batch *batch, int32_t bubbles_per_block);
 /* Autotuner: times `steps_per_trial` steps (these advance the foams) with
- * each candidate tile (512 ... 8192 bubbles per block), keeps the fastest
- * and returns it in *tile. */
+ * each candidate tile (512 ... 8192 bubbles per block), then with each
+ * cell_scale and, in the mixed form, each pair_run candidate of cb_tuning
+ * (applied to every foam), keeps the fastest of each and returns the tile in
+ * *tile (the other knobs: cb_get_tuning of any foam's context). */
 CB_API int cb_batch_autotune(cb_batch *batch, int32_t steps_per_trial, int32_t *tile);
+/* Applies the knobs of cb_tuning to every foam of the batch. */
+CB_API int cb_batch_set_tuning(cb_batch *batch, const cb_tuning *tuning);
 CB_API int cb_batch_launch_count(cb_batch *batch, int64_t *count);
 
 /* Total potential energy of a foam, as cb_energy computes it, for callers

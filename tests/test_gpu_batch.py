@@ -166,7 +166,8 @@ def test_batch_autotune_keeps_results():
     tile = batch.autotune(3)
     assert tile in (512, 1024, 2048, 4096, 8192)
     reps = batch.integrate(5)
+    # trials of 3 steps: 5 tiles, 3 cell scales, 3 pairs-per-thread values
     for f, r in enumerate(reps):
-        assert r["steps"] - r0[f] == 5 * 3 + 5
+        assert r["steps"] - r0[f] == (5 + 3 + 3) * 3 + 5
         assert r["status"] == 0
     batch.close()
