@@ -341,6 +341,9 @@ def measure_form(args, world, rank, precision, clocks_on=True):
     sim = cb.GpuFoam(cfg)
     sim.load_state(st)
     workloads.prepare(sim)
+    # launch and search knobs picked by the autotuner on the prepared foam
+    # (kept for the later contexts of this kind in the process)
+    tuning = sim.autotune(3) if args.autotune else sim.tuning()
     sim.integrate(args.warmup)
     r0 = sim.report()
     l0 = sim.launch_count()
@@ -418,7 +421,8 @@ def measure_form(args, world, rank, precision, clocks_on=True):
     sim.close()
     return {"value": bs_all / el, "el": el, "cfg": cfg, "st": st, "desc": desc, "r0": r0,
             "r1": r1, "roofline": roof, "launches": launches, "clocks": clk,
-            "np_per_n": np_per_n, "amortised": amort, "search_ms": search_ms}
+            "np_per_n": np_per_n, "amortised": amort, "search_ms": search_ms,
+            "tuning": tuning}
 
 
 def form_errors(args, precision=1, steps=50):
@@ -600,7 +604,13 @@ def batch_errors(items, steps=50):
     r64, rmx = b64.integrate(steps), bmx.integrate(steps)
     out = {"steps": steps, "foams": len(items), "same_attempts_searches_deletions": True,
            "foams_with_same_counts": 0, "dx": 0.0, "r": 0.0, "volume_drift": 0.0,
-           "deleted_fp64": 0, "deleted_mixed": 0}
+           "volume_vs_target_fp64": 0.0, "volume_vs_target_mixed": 0.0,
+           "deleted_fp64": 0, "deleted_mixed": 0,
+           "note": "volume_drift compares the two runs; volume_vs_target_* is each run's own "
+                   "total gas volume against pi M^2, the value every deletion's volume fix "
+                   "restores (src/kernels.cu:859-867): the AM2 update keeps it to first order "
+                   "in dt only, so both runs drift between deletions, and runs whose "
+                   "deletions fall on different steps differ by that drift"}
     for f, ((cfg, _), f64, fmx) in enumerate(zip(items, b64.foams, bmx.foams)):
         same = all(r64[f][k] == rmx[f][k] for k in ("attempts", "searches", "deleted"))
         out["same_attempts_searches_deletions"] &= same
@@ -623,6 +633,9 @@ def batch_errors(items, steps=50):
                                         np.max(np.abs(a["r"]))))
         v64, vmx = f64.total_volume(), fmx.total_volume()
         out["volume_drift"] = max(out["volume_drift"], abs(vmx - v64) / v64)
+        vt = math.pi * cfg.bubble_volume_multiplier ** 2
+        out["volume_vs_target_fp64"] = max(out["volume_vs_target_fp64"], abs(v64 / vt - 1.0))
+        out["volume_vs_target_mixed"] = max(out["volume_vs_target_mixed"], abs(vmx / vt - 1.0))
     b64.close()
     bmx.close()
     return out
@@ -645,6 +658,7 @@ def measure_batch(args, world, rank):
         workloads.prepare(f)
     setup_s = time.perf_counter() - t0
     tile = batch.autotune(args.batch_tune_steps)
+    tuning = batch.foams[0].tuning()
     batch.integrate(args.warmup)
     r0 = [f.report() for f in batch.foams]
     l0 = batch.launch_count()
@@ -667,6 +681,7 @@ def measure_batch(args, world, rank):
            "ms_per_batch_step": ms / args.batch_steps,
            "foams": len(items), "bubbles": int(sum(st["x"].size for _, st in items)),
            "steps_each": args.batch_steps, "tile_bubbles_per_block": tile,
+           "tuning": tuning,
            "attempts": sum(r["attempts"] - q["attempts"] for r, q in zip(reps, r0)),
            "searches": sum(r["searches"] - q["searches"] for r, q in zip(reps, r0)),
            "deleted": sum(r["deleted"] - q["deleted"] for r, q in zip(reps, r0)),
@@ -758,6 +773,43 @@ def reference_cuda(args, steps):
     return out
 
 
+def measure_sheared(args):
+    """A sample of the large sheared foam (3D, N = 1e7, walls in z, linear
+    shear along x, mixed form): `--c5-steps` accepted steps after its search,
+    bootstrap and warm-up, one graph launch, CUDA events. The run until half
+    the bubbles are deleted (`--workload c5 --until-deleted 0.5`) takes
+    minutes and is reported from its own runs."""
+    import torch
+    import cubble_gb300 as cb
+    from cubble_gb300 import workloads
+    n = args.c5_n
+    t0 = time.perf_counter()
+    cfg, st = workloads.config_c5(n=n, precision=1, use_graph=1)
+    free0, _ = torch.cuda.mem_get_info()
+    sim = cb.GpuFoam(cfg)
+    sim.load_state(st)
+    free1, _ = torch.cuda.mem_get_info()
+    workloads.prepare(sim)
+    sim.integrate(args.warmup)
+    setup_s = time.perf_counter() - t0
+    r0 = sim.report()
+    r1, ms = sim.integrate_timed(args.c5_steps)
+    out = {"value": (r1["bubble_steps"] - r0["bubble_steps"]) / (ms / 1e3),
+           "unit": "bubble-steps/s", "steps": r1["steps"] - r0["steps"],
+           "ms_per_step": ms / max(r1["steps"] - r0["steps"], 1),
+           "attempts": r1["attempts"] - r0["attempts"],
+           "searches": r1["searches"] - r0["searches"],
+           "deleted": r1["deleted"] - r0["deleted"],
+           "bubbles_start": n, "bubbles_end": r1["count"],
+           "device_bytes_held": int(free0 - free1), "setup_s": setup_s,
+           "workload": "3D foam N=%d, walls in z, periodic x/y, linear shear along x (max "
+                       "speed 0.05), phi=0.80, r~N(1,0.15) in [0.3,2.5], kappa=0.01, K=0.1, "
+                       "tol 1e-5, mixed precision; a %d-step sample of the run to 50%% "
+                       "deleted" % (n, args.c5_steps)}
+    sim.close()
+    return out
+
+
 def run_gb300(args, world, rank, local):
     import torch
     import cubble_gb300 as cb
@@ -785,8 +837,11 @@ def run_gb300(args, world, rank, local):
         workloads.prepare(g2)
         t2 = time.perf_counter()
         q0 = g2.report()
+        calls = []
         for _ in range(args.warmup + args.steps):
+            tc = time.perf_counter()
             g2.integrate(1)
+            calls.append(1e3 * (time.perf_counter() - tc))
         q1 = g2.report()
         t3 = time.perf_counter()
         fin = g2.get_state(rows=list(host.keys()), out=down)
@@ -794,7 +849,9 @@ def run_gb300(args, world, rank, local):
         t4 = time.perf_counter()
         e2e_s = t4 - t0
         parts = {"upload_ms": 1e3 * (t1 - t0), "search_bootstrap_ms": 1e3 * (t2 - t1),
-                 "steps_ms": 1e3 * (t3 - t2), "download_ms": 1e3 * (t4 - t3)}
+                 "steps_ms": 1e3 * (t3 - t2), "download_ms": 1e3 * (t4 - t3),
+                 "call_ms_first": calls[:3], "call_ms_median": statistics.median(calls),
+                 "attempts": q1["attempts"] - q0["attempts"]}
         barrier(world)
         e2e_s = allreduce(e2e_s, _op("max"), world)
         e2e_bs = allreduce(q1["bubble_steps"] - q0["bubble_steps"], _op("sum"), world)
@@ -819,6 +876,7 @@ def run_gb300(args, world, rank, local):
                  "attempts": mx["r1"]["attempts"] - mx["r0"]["attempts"],
                  "searches": mx["r1"]["searches"] - mx["r0"]["searches"],
                  "roofline": mx["roofline"], "gpu_launches": mx["launches"],
+                 "tuning": mx["tuning"],
                  "workload": "same foam, mixed precision: FP32 pair geometry on exact 64-bit "
                              "fixed-point differences, FP32 rates; FP64 positions, radii, "
                              "volume sum and fix, error norm, energy"}
@@ -850,6 +908,10 @@ def run_gb300(args, world, rank, local):
     if not args.no_batch:
         batched = measure_batch(args, world, rank)
 
+    sheared = None
+    if args.c5_steps > 0:
+        sheared = measure_sheared(args)
+
     ref_cuda = None
     if rank == 0 and args.ref_cuda_steps > 0:
         try:
@@ -879,6 +941,7 @@ def run_gb300(args, world, rank, local):
                    "attempts": attempts, "searches": searches,
                    "steps_per_search": (args.steps / searches) if searches else None,
                    "pairs_per_bubble": main["np_per_n"], "bubbles_end": r1["count"],
+                   "tuning": main["tuning"],
                    "deleted": r1["deleted"] - r0["deleted"], "dt_end": r1["time_step"]},
         "search": {"search_ms": main["search_ms"],
                    "what": "device time of one neighbour search of the N-bubble foam "
@@ -886,7 +949,7 @@ def run_gb300(args, world, rank, local):
         "amortised": main["amortised"], "reference_cuda": ref_cuda,
         "roofline": main["roofline"], "cpu_baseline": base, "e2e": e2e,
         "gpu_launches": main["launches"], "clocks": main["clocks"], "mixed": mixed,
-        "fp64_ff": fp64_ff, "batched": batched,
+        "fp64_ff": fp64_ff, "batched": batched, "sheared": sheared,
     }
     print(json.dumps(line))
 
@@ -927,6 +990,11 @@ def main():
     ap.add_argument("--long-steps", type=int, default=2000)
     ap.add_argument("--long-every", type=int, default=100)
     ap.add_argument("--batch-error-steps", type=int, default=5000)
+    # 1: the autotuner picks the cb_tuning knobs before the warm-up
+    ap.add_argument("--autotune", type=int, default=1)
+    # the large sheared foam's sample: bubbles and accepted steps (0: off)
+    ap.add_argument("--c5-n", type=int, default=10_000_000)
+    ap.add_argument("--c5-steps", type=int, default=1000)
     ap.add_argument("--until-deleted", type=float, default=0.0)
     ap.add_argument("--chunk-steps", type=int, default=2000)
     ap.add_argument("--max-run-steps", type=int, default=200000)
