@@ -242,6 +242,7 @@ int build_batch_graph(cb_batch *b) {
     launch_batch_search(b, &dummy);
     CB_CUDA(cudaStreamEndCapture(s, &out));
     CB_CUDA(cudaGraphInstantiate(&b->gexec, g, 0));
+    CB_CUDA(cudaGraphUpload(b->gexec, b->stream));
     CB_CUDA(cudaGraphDestroy(g));
     b->graph_tile = b->tile;
     b->hbc->h_loop = (unsigned long long)hloop;

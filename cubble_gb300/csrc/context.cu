@@ -282,6 +282,8 @@ int build_graph(cb_context *c) {
     launch_search(l, c->bufs, dim);
     CB_CUDA(cudaStreamEndCapture(s, &out));
     CB_CUDA(cudaGraphInstantiate(&c->gexec, g, 0));
+    // upload now, so that the first integrate's launch does not carry it
+    CB_CUDA(cudaGraphUpload(c->gexec, c->stream));
     CB_CUDA(cudaGraphDestroy(g));
     c->graph_key = key;
     int r2 = c->pull();

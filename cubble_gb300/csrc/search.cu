@@ -55,6 +55,41 @@ __device__ __forceinline__ int cell_coord(double x, double lbb, double iv, int c
     const double q = floor(__ddiv_rn(__dmul_rn((double)cd, __dsub_rn(x, lbb)), iv));
     return q < 0.0 ? 0 : (q >= (double)cd ? cd - 1 : (int)q);
 }
+__device__ __noinline__ int cell_coord_slow(double x, double lbb, double iv, int cd) {
+    return cell_coord(x, lbb, iv, cd);
+}
+
+// The same cell coordinate with the FP64 division (about ten FP64-pipe
+// instructions) only where it matters: q = cd (x - lbb) / iv in FP32 from the
+// truncated x is within `band` of the FP64 value (|x - x32| <= 2^-23 |x|,
+// three FP32 roundings of 2^-24 each), so unless its fractional part lies
+// within `band` of a cell face, or outside the grid, its floor is the FP64
+// expression's floor.
+struct CellAxis {
+    float lbb, scale, band;
+    double lbb_d, iv;
+    int cd;
+};
+
+__device__ __forceinline__ CellAxis cell_axis(const DevConst &k, int a, int cd) {
+    CellAxis c;
+    c.lbb = k.lbb_f[a];
+    c.scale = (float)cd / k.iv32[a];
+    const float ma = fmaxf(fabsf(k.lbb_f[a]), fabsf(k.lbb_f[a] + k.iv32[a]));
+    c.band = 9.5367431640625e-07f * (float)cd * (1.f + ma / k.iv32[a]);  // 2^-20 cd (1 + |x|/L)
+    c.lbb_d = k.lbb[a];
+    c.iv = k.iv[a];
+    c.cd = cd;
+    return c;
+}
+
+__device__ __forceinline__ int cell_coord_fast(double x, const CellAxis &c) {
+    const float q = (ff_f32(x) - c.lbb) * c.scale;
+    const float fl = floorf(q);
+    const float fr = q - fl;
+    if (fr > c.band && fr < 1.f - c.band && fl >= 0.f && fl < (float)c.cd) return (int)fl;
+    return cell_coord_slow(x, c.lbb_d, c.iv, c.cd);
+}
 
 template <int DIM>
 __device__ __forceinline__ void k_wrap_body(const Bufs &b, const int vb, const int vg) {
@@ -65,12 +100,22 @@ __device__ __forceinline__ void k_wrap_body(const Bufs &b, const int vb, const i
     double *XR[3] = {drow(b, c, RX), drow(b, c, RY), drow(b, c, RZ)};
     int *WR[3] = {irow(b, c, IWX), irow(b, c, IWY), irow(b, c, IWZ)};
     const double *R = drow(b, c, RR);
+    // box constants in registers: the stores below may alias them for the
+    // compiler, which would reload them per bubble
+    bool per[3];
+    double lo3[3], hi3[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        per[a] = a < DIM && !k.wall[a];
+        lo3[a] = k.lbb[a];
+        hi3[a] = k.tfr[a];
+    }
     double mr = 0.0;
     for (int i = vb * blockDim.x + threadIdx.x; i < n; i += vg * blockDim.x) {
 #pragma unroll
         for (int a = 0; a < DIM; a++) {
-            if (k.wall[a]) continue;
-            const double lo = k.lbb[a], hi = k.tfr[a];
+            if (!per[a]) continue;
+            const double lo = lo3[a], hi = hi3[a];
             const double x = XR[a][i];
             const int mult = x < lo ? 1 : (x > hi ? -1 : 0);
             if (mult) {
@@ -116,10 +161,12 @@ __device__ __forceinline__ void k_cell_count_body(const Bufs &b, const int vb, c
     const int n = c->n;
     const int cd0 = c->cell_dims[0], cd1 = c->cell_dims[1], cd2 = c->cell_dims[2];
     const double *X = drow(b, c, RX), *Y = drow(b, c, RY), *Z = drow(b, c, RZ);
+    const CellAxis ax = cell_axis(k, 0, cd0), ay = cell_axis(k, 1, cd1);
+    const CellAxis az = cell_axis(k, 2, DIM == 3 ? cd2 : 1);
     for (int i = vb * blockDim.x + threadIdx.x; i < n; i += vg * blockDim.x) {
-        const int kx = cell_coord(X[i], k.lbb[0], k.iv[0], cd0);
-        const int ky = cell_coord(Y[i], k.lbb[1], k.iv[1], cd1);
-        const int kz = DIM == 3 ? cell_coord(Z[i], k.lbb[2], k.iv[2], cd2) : 0;
+        const int kx = cell_coord_fast(X[i], ax);
+        const int ky = cell_coord_fast(Y[i], ay);
+        const int kz = DIM == 3 ? cell_coord_fast(Z[i], az) : 0;
         const int ci = (kz * cd1 + ky) * cd0 + kx;
         b.cellOf[i] = ci;
         atomicAdd(b.cellCount + ci, 1);
@@ -614,12 +661,37 @@ __device__ __forceinline__ void k_pair_compact_body(const Bufs &b, const int vb,
     const int pcap = b.k->pcap;
     int *PI = b.ps[c->prole[PI0]];
     int *PJ = b.ps[c->prole[PJ0]];
-    for (int i = vb * blockDim.x + threadIdx.x; i < n; i += vg * blockDim.x) {
-        const int base = b.rowStart[i], cnt = b.rowCount[i];
-        const int *src = b.stash + (size_t)i * M;
-        for (int t = 0; t < cnt && base + t < pcap; t++) {
-            PI[base + t] = i;
-            PJ[base + t] = src[t];
+    // A warp writes the contiguous output range of its 32 rows, 32 slots at
+    // a time (coalesced); the row of a slot is the last of the 32 rows
+    // starting at or before it (binary search over the lanes' row starts).
+    // Every loop bound is uniform over the warp, so all lanes take part in
+    // each shuffle.
+    const int lane = threadIdx.x & 31;
+    int *NN = b.is[c->irole[INN]];
+    for (int i0 = vb * blockDim.x + (threadIdx.x & ~31); i0 < n; i0 += vg * blockDim.x) {
+        const int i = i0 + lane;
+        const bool act = i < n;
+        const int st = act ? b.rowStart[i] : 0;
+        const int ct = act ? b.rowCount[i] : 0;
+        const int last = min(31, n - 1 - i0);
+        const int lo = __shfl_sync(0xffffffffu, st, 0);
+        const int hi = __shfl_sync(0xffffffffu, st + ct, last);
+        for (int o0 = lo; o0 < hi; o0 += 32) {
+            const int o = o0 + lane;
+            int r = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+                const int cand = r + step;
+                const int sc = __shfl_sync(0xffffffffu, st, cand & 31);
+                if (cand <= last && sc <= o) r = cand;
+            }
+            const int sr = __shfl_sync(0xffffffffu, st, r);
+            if (o < hi && o < pcap) {
+                const int j = b.stash[(size_t)(i0 + r) * M + (o - sr)];
+                PI[o] = i0 + r;
+                PJ[o] = j;
+                atomicAdd(NN + j, 1);  // j's degree (countNumNeighbors); i's came with the row
+            }
         }
     }
     if (last_block(&c->done[DC_MISC], vg) && threadIdx.x == 0) {
@@ -637,8 +709,11 @@ __device__ __forceinline__ void k_pair_compact_body(const Bufs &b, const int vb,
 CB_KERNEL_PAIR((template <int DIM>), k_pair_compact, (<DIM>), __launch_bounds__(kBlock))
 
 
+// j-side neighbour counts of a list the second enumeration wrote (the
+// compaction counts them itself when it writes the list).
 __device__ __forceinline__ void k_degree_body(const Bufs &b, const int vb, const int vg) {
     const Ctrl *c = b.ctrl;
+    if (!c->stash_over) return;
     const int np = c->np;
     const int *PJ = b.ps[c->prole[PJ0]];
     int *NN = b.is[c->irole[INN]];
