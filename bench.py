@@ -397,6 +397,9 @@ def measure_form(args, world, rank, precision, clocks_on=True):
              else "k_correct<%d>" % dim)
     kpairs = "k_pairs%s<%d, %d, %d>" % (sfx if mixed else ("_ff" if precision == 2 else ""),
                                         dim, gas, flow)
+    if mixed:  # the mixed pair kernel's pairs per thread (a template argument)
+        run = tuning["pair_run"] if (gas and not flow) else 4
+        kpairs = "k_pairs_mx<%d, %d, %d, %d>" % (dim, gas, flow, run)
     kname = {"predict": "k_predict%s<%d>" % (sfx, dim), "correct": kcorr,
              "pairs": kpairs}[names[top]]
     tr = profiled_traffic(kname)

@@ -16,6 +16,9 @@ Bars:
     exact;
   * 10 accepted steps: the same attempt, search and deletion counts and
     dt, every state row within 1e-9;
+  * 60 accepted steps in lockstep, compared after every step (counts, dt,
+    pair count, positions, radii and rates within 1e-9), through at least
+    one neighbour search;
   * the mixed form's attempt on the oracle's state: positions (their
     change), velocities, radius rates, overlap areas and path increments
     within 1e-6 of each row's largest magnitude, the global sums within
@@ -135,5 +138,30 @@ def test_c2_mixed_attempt(oracle_mod, c2):
     tol = cfg.error_tolerance
     assert abs(ag["max_error"] - ao["max_error"]) <= lim * tol
     assert np.array_equal(ag["delete_flags"], ao["delete_flags"])
+    g.close()
+    o.close()
+
+
+def test_c2_every_step(oracle_mod, c2):
+    """60 accepted steps of the 3D N = 10^6 foam with the CUDA path and the
+    oracle in lockstep, compared after every step: the same attempt, search
+    and deletion counts, dt and pair count, and positions, radii and their
+    rates within 1e-9 of each row's maximum, by bubble index. The window
+    holds at least one neighbour search."""
+    cfg, st = c2
+    g, o = both(oracle_mod, cfg, st)
+    for f in (g, o):
+        workloads.prepare(f)
+    rows = ["x", "y", "z", "r", "dxdt", "dydt", "dzdt", "drdt", "index"]
+    s0 = g.report()["searches"]
+    for step in range(60):
+        rg, ro = g.integrate(1), o.integrate(1)
+        for k in ("steps", "attempts", "searches", "deleted", "count", "num_pairs"):
+            assert rg[k] == ro[k], (step, k)
+        assert rg["time_step"] == pytest.approx(ro["time_step"], rel=1e-12), step
+        sg, so = by_index(g.get_state(rows=rows)), by_index(o.get_state(rows=rows))
+        assert np.array_equal(sg["index"], so["index"]), step
+        assert_rows_close(sg, so, rows[:-1], 1e-9, "step %d " % step)
+    assert g.report()["searches"] > s0
     g.close()
     o.close()
