@@ -91,9 +91,14 @@ void fill_const(cb_context *c) {
         k.lq[a] = (long long)std::llround(k.iv[a] * 1099511627776.0);  // 2^40
         k.hq[a] = k.lq[a] / 2;
     }
-    // FP32 coordinates carry |x| 2^-24 rounding; 1e-5 (maxabs + interval) is
-    // more than 20x the worst error of the prefiltered distance.
-    k.pre_margin = (float)(1e-5 * (maxabs + maxiv) + 1e-4);
+    // Guard band of the FP32 pair prefilters. An FP32 coordinate carries up
+    // to 2^-24 |x| rounding, a periodic shift or minimum image another
+    // 2^-24 (|x| + L) (the box edge L rounded to FP32, the shifted value
+    // rounded), so a difference is off by at most 2^-24 (3 maxabs + 2 L)
+    // per axis, the distance by sqrt(3) times that: < 5.2e-7 (maxabs + L).
+    // The squared-distance and cutoff roundings add < 1e-6 absolute.
+    // 2e-6 (maxabs + L) + 1e-5 is about 4x the worst case.
+    k.pre_margin = (float)(2e-6 * (maxabs + maxiv) + 1e-5);
     k.shear_on = f.shear_speed != 0.0 ? 1 : 0;
     k.shear_axis = k.dim - 1;
     k.shear = f.shear_speed;

@@ -513,13 +513,24 @@ __device__ __forceinline__ void k_pair_cells_body(const Bufs &b, const int vb, c
 }
 CB_KERNEL_PAIR((template <int DIM, bool WRITE>), k_pair_cells, (<DIM, WRITE>), __launch_bounds__(kBlock))
 
-// Counting pass for sparse cell grids (fewer than 24 bubbles per cell on
-// average: 2D foams, and 3D foams whose cell edge 2 maxR + skin holds ~10
-// bubbles): one thread per bubble walks its neighbour cells
-// >= its own cell in ascending order and the bubbles j > i in them, so the
-// rows and their order are those of the warp-per-cell pass, with all lanes
-// busy (a warp per cell of ~3 bubbles would leave 90 % of its lanes idle;
-// measured on GB300 the thread pass is faster up to at least 10 per cell).
+// Sparse 3D grids whose periodic axes have at least four cells (and fewer
+// than 2^25 cells) are counted by k_pair_tiles: a neighbour cell is then
+// reached through at most one periodic image, and never twice.
+template <int DIM>
+__device__ __forceinline__ bool tile_grid(const DevConst &k, const int cd[3], int ncell) {
+    bool ok = DIM == 3 && ncell < (1 << 25);  // cell index and shift in one sort key
+#pragma unroll
+    for (int a = 0; a < DIM; a++) ok &= k.wall[a] || cd[a] >= 4;
+    return ok;
+}
+
+// Counting pass for sparse 2D cell grids (fewer than 24 bubbles per cell on
+// average; 2D cells hold ~3) and the sparse 3D grids k_pair_tiles does not
+// take (an axis with fewer than four cells): one thread per bubble walks its
+// neighbour cells >= its own cell in ascending order and the bubbles j > i
+// in them, so the rows and their order are those of the warp-per-cell pass,
+// with all lanes busy (a warp per cell of ~3 bubbles would leave 90 % of its
+// lanes idle).
 template <int DIM>
 __device__ __forceinline__ void k_pair_rows_body(const Bufs &b, const int vb, const int vg) {
     Ctrl *c = b.ctrl;
@@ -538,16 +549,7 @@ __device__ __forceinline__ void k_pair_rows_body(const Bufs &b, const int vb, co
 #pragma unroll
     for (int a = 0; a < 3; a++) cw[a] = k.iv32[a] / (float)cd[a];
     const float reach0 = c->search_maxr + k.skin_f + k.pre_margin + 1e-3f;
-    // with at least four cells on every periodic axis a listed cell's
-    // candidates lie within half a box of the bubble's image for that cell:
-    // the bubble is moved by the cell's image shift once, and candidates are
-    // tested on plain differences (no minimum image per candidate). 3D only:
-    // 2D cells hold ~3 bubbles, and the shift per cell then costs more than
-    // the minimum image per candidate (measured on GB300: 3D N = 10^6 search
-    // 0.966 -> 0.926 ms, 2D 1.042 -> 1.080 ms)
-    bool direct = DIM == 3;
-#pragma unroll
-    for (int a = 0; a < DIM; a++) direct &= k.wall[a] || cd[a] >= 4;
+    if (DIM == 3 && tile_grid<DIM>(k, cd, c->ncell)) return;  // k_pair_tiles counts it
     bool over = false;
     for (int i = vb * blockDim.x + threadIdx.x; i < n; i += vg * blockDim.x) {
         const int cell = b.cellSorted[i];
@@ -564,7 +566,6 @@ __device__ __forceinline__ void k_pair_rows_body(const Bufs &b, const int vb, co
             hi[a] = fmaxf((float)(kk[a] + 1) * cw[a] - pr[a], 0.f);
         }
         int nb[NO];
-        int ns[NO];  // image shift per listed cell: 2 bits per axis, 1 = +L, 2 = -L
         int nq = 0;
 #pragma unroll
         for (int t = 0; t < NO; t++) {
@@ -572,7 +573,6 @@ __device__ __forceinline__ void k_pair_rows_body(const Bufs &b, const int vb, co
             const int off[3] = {o % 3 - 1, (o / 3) % 3 - 1, o / 9 - 1};
             // neighbour cell index (getNeighborCellIndex, src/kernels.cu:1157-1189)
             int q[3];
-            int sh = 0;
             bool ok = true;
 #pragma unroll
             for (int a = 0; a < 3; a++) {
@@ -583,7 +583,6 @@ __device__ __forceinline__ void k_pair_rows_body(const Bufs &b, const int vb, co
                 } else if (!k.wall[a]) {
                     ok &= !(d == 1 && off[a] != 0) && !(d == 2 && off[a] == -1);
                     q[a] = kk[a] + off[a];
-                    sh |= (q[a] < 0 ? 1 : (q[a] >= d ? 2 : 0)) << (2 * a);
                     q[a] = q[a] < 0 ? q[a] + d : (q[a] >= d ? q[a] - d : q[a]);
                 } else {
                     q[a] = kk[a] + off[a];
@@ -606,11 +605,9 @@ __device__ __forceinline__ void k_pair_rows_body(const Bufs &b, const int vb, co
             int p = nq++;  // insertion into the ascending list
             while (p > 0 && nb[p - 1] > v) {
                 nb[p] = nb[p - 1];
-                ns[p] = ns[p - 1];
                 p--;
             }
             nb[p] = v;
-            ns[p] = sh;
         }
         // the candidates of all listed cells as one flat sequence: a lane
         // moves to its next cell inside the loop, so the warp runs for its
@@ -618,22 +615,15 @@ __device__ __forceinline__ void k_pair_rows_body(const Bufs &b, const int vb, co
         // longest lane's count in each
         int cnt = 0;
         int t = -1, j = 0, je = 0;
-        float4 ps = pi;
         while (true) {
             while (j >= je && ++t < nq) {
                 const int qc = nb[t];
                 j = max(b.cellStart[qc], i + 1);
                 je = b.cellStart[qc + 1];
-                const int sh = ns[t];
-                const float s[3] = {
-                    (sh & 1) ? k.iv32[0] : ((sh & 2) ? -k.iv32[0] : 0.f),
-                    (sh & 4) ? k.iv32[1] : ((sh & 8) ? -k.iv32[1] : 0.f),
-                    (sh & 16) ? k.iv32[2] : ((sh & 32) ? -k.iv32[2] : 0.f)};
-                ps = make_float4(pi.x + s[0], pi.y + s[1], pi.z + s[2], pi.w);
             }
             if (t >= nq) break;
             const float4 pj = b.pos32[j];
-            const int cls = direct ? pair_class_direct<DIM>(k, ps, pj) : pair_class<DIM>(k, pi, pj);
+            const int cls = pair_class<DIM>(k, pi, pj);
             if (cls == 1 || (cls == 2 && pair_take_exact<DIM>(k, i, j, X, Y, Z, R))) {
                 if (cnt < M) b.stash[(size_t)i * M + cnt] = j;
                 cnt++;
@@ -647,6 +637,231 @@ __device__ __forceinline__ void k_pair_rows_body(const Bufs &b, const int vb, co
     if (__syncthreads_or(over) && threadIdx.x == 0) atomicOr(&c->stash_over, 1);
 }
 CB_KERNEL_PAIR((template <int DIM>), k_pair_rows, (<DIM>), __launch_bounds__(kBlock))
+
+// Counting pass for sparse 3D grids with at least four cells on every
+// periodic axis, one warp per home cell. The candidates of the cell (its own
+// bubbles and those of its neighbour cells >= it, cells ascending, bubbles
+// ascending inside a cell) are laid over the lanes 32 at a time, each lane
+// loading one candidate (a cell's bubbles are contiguous, so the loads are
+// coalesced) and moving it by its cell's periodic image shift into the home
+// cell's frame (four or more cells per axis make the shift unique, and
+// candidates are tested on plain differences). The home cell's bubbles are
+// then broadcast from shared memory one at a time and every lane tests its
+// candidate against the bubble; the warp's hit mask of each (bubble, chunk)
+// goes to shared memory, and after a window of up to kTileChunks chunks each
+// lane walks the masks of its home bubble and appends the partners to the
+// bubble's row in candidate order, the order of the thread pass, so stash,
+// counts and pair list are the same. All lanes work on every test, against
+// a thread per bubble that walks its own cells with, in 3D, less than half
+// of its warp's lanes busy.
+constexpr int kTileChunks = 16;  // candidate window: 16 chunks of 32
+
+// The tests of one chunk against home bubbles 0..nh-1 (home cell bubbles
+// among the candidates: CMP, the j > i order test): the warp's hit mask of
+// each home bubble goes to masks[a]. Tests in the guard band (d2 - cut^2
+// within +-tb of zero, tb = 2 cutmax band >= 2 cut band; 2 cut band + band^2
+// would be the exact band, the narrower one is within its margin) are only
+// flagged here; the return value says whether any lane had one, and
+// tile_exact then decides them.
+template <bool CMP>
+__device__ __forceinline__ bool tile_tests(const float4 *home, int nh, int h0, int j,
+                                           const float4 &pj, float wj, float tb,
+                                           unsigned *masks) {
+    unsigned amb_any = 0;
+#pragma unroll 4
+    for (int a = 0; a < nh; a++) {
+        const float4 pi = home[a];
+        const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+        const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        const float cut = pi.w + wj;
+        const float e = fmaf(-cut, cut, d2);
+        bool take = e < -tb, amb = e < tb;
+        if (CMP) {
+            take &= j > h0 + a;
+            amb &= j > h0 + a;
+        }
+        masks[a] = __ballot_sync(0xffffffffu, take);
+        amb_any |= __ballot_sync(0xffffffffu, amb && !take);
+    }
+    return amb_any != 0;
+}
+// The FP64 test of the reference for the guard-band pairs of a chunk: the
+// chunk's tests are repeated and each band pair's bit set by the exact
+// decision (comparePair, src/kernels.cu:619-623).
+template <int DIM>
+static __device__ __noinline__ void tile_exact(const DevConst &k, const float4 *home, int nh,
+                                               int h0, int j, float4 pj, float wj, float tb,
+                                               unsigned *masks, const double *X,
+                                               const double *Y, const double *Z,
+                                               const double *R) {
+    const int lane = threadIdx.x & 31;
+    __syncwarp();
+    for (int a = 0; a < nh; a++) {
+        const float4 pi = home[a];
+        const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+        const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        const float cut = pi.w + wj;
+        const float e = fmaf(-cut, cut, d2);
+        const bool amb = j > h0 + a && !(e < -tb) && e < tb;
+        if (amb && pair_take_exact<DIM>(k, h0 + a, j, X, Y, Z, R))
+            atomicOr(masks + a, 1u << lane);
+    }
+    __syncwarp();
+}
+
+template <int DIM>
+__device__ __forceinline__ void k_pair_tiles_body(const Bufs &b, const int vb, const int vg) {
+    __shared__ float4 home[kWarpsPerBlock][32];
+    __shared__ unsigned hitmask[kWarpsPerBlock][kTileChunks][32];  // [chunk][home bubble]
+    __shared__ int candj[kWarpsPerBlock][kTileChunks * 32];
+    Ctrl *c = b.ctrl;
+    if (!c->sparse_cells) return;
+    const DevConst &k = *b.k;
+    const int cd[3] = {c->cell_dims[0], c->cell_dims[1], c->cell_dims[2]};
+    const int ncell = c->ncell;
+    if (!tile_grid<DIM>(k, cd, ncell)) return;  // k_pair_rows counts it
+    constexpr int M = kStash(DIM);
+    constexpr unsigned kAll = 0xffffffffu;
+    const double *X = drow(b, c, RX), *Y = drow(b, c, RY), *Z = drow(b, c, RZ),
+                 *R = drow(b, c, RR);
+    int *NN = irow(b, c, INN);
+    int *stash = b.stash, *rowCount = b.rowCount;
+    const int *cellStart = b.cellStart;
+    const float4 *pos = b.pos32;
+    // constants in registers (a store through `stash` could alias them)
+    // the guard band in d2 - cut^2 units: 2 cut band for the largest cut
+    const float skin = k.skin_f;
+    const float tb = 2.f * k.pre_margin * (2.f * (c->search_maxr + 1e-3f) + skin);
+    const float L[3] = {k.iv32[0], k.iv32[1], k.iv32[2]};
+    const bool per[3] = {!k.wall[0], !k.wall[1], !k.wall[2]};
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int plane = cd[0] * cd[1];
+    const int warps = vg * kWarpsPerBlock;
+    bool over = false;
+    for (int cell = vb * kWarpsPerBlock + w; cell < ncell; cell += warps) {
+        const int s0 = cellStart[cell], e0 = cellStart[cell + 1];
+        if (s0 == e0) continue;
+        // lane t < m: the t-th neighbour cell >= cell in ascending order
+        // (getNeighborCellIndex, src/kernels.cu:1157-1189) with its periodic
+        // image shift in the low 6 bits of the key (2 bits per axis: 1 =
+        // reached below 0, the candidate is moved by -L; 2 = reached above
+        // the box, moved by +L). Away from the box faces these are the
+        // offsets 13..26 of the 27-cell stencil in order, with no shift.
+        const int hk[3] = {cell % cd[0], (cell / cd[0]) % cd[1], cell / plane};
+        const bool inner = hk[0] >= 1 && hk[0] <= cd[0] - 2 && hk[1] >= 1 &&
+                           hk[1] <= cd[1] - 2 && hk[2] >= 1 && hk[2] <= cd[2] - 2;
+        int key = 0x7fffffff, m = 14;
+        if (inner) {
+            if (lane < 14) {
+                const int o = 13 + lane;
+                key = (cell + (o / 9 - 1) * plane + ((o / 3) % 3 - 1) * cd[0] + (o % 3 - 1)) << 6;
+            }
+        } else {
+            if (lane < 27) {
+                const int off[3] = {lane % 3 - 1, (lane / 3) % 3 - 1, lane / 9 - 1};
+                int q[3], sh = 0;
+                bool ok = true;
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    q[a] = hk[a] + off[a];
+                    if (per[a]) {
+                        if (q[a] < 0) {
+                            q[a] += cd[a];
+                            sh |= 1 << (2 * a);
+                        } else if (q[a] >= cd[a]) {
+                            q[a] -= cd[a];
+                            sh |= 2 << (2 * a);
+                        }
+                    } else {
+                        ok &= q[a] >= 0 && q[a] < cd[a];
+                    }
+                }
+                const int v = (q[2] * cd[1] + q[1]) * cd[0] + q[0];
+                if (ok && v >= cell) key = (v << 6) | sh;
+            }
+            key = warp_sort(key);
+            m = __popc(__ballot_sync(kAll, key != 0x7fffffff));
+        }
+        int cs = 0, cn = 0;
+        if (lane < m) {
+            const int v = key >> 6;
+            cs = cellStart[v];
+            cn = cellStart[v + 1] - cs;
+        }
+        int pre = cn;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(kAll, pre, o);
+            if (lane >= o) pre += t;
+        }
+        const int T = __shfl_sync(kAll, pre, 31);  // lanes >= m add nothing
+        const int nhome = e0 - s0;                  // the home cell is the first
+        for (int h0 = s0; h0 < e0; h0 += 32) {
+            const int nh = min(32, e0 - h0);
+            __syncwarp();
+            if (lane < nh) home[w][lane] = pos[h0 + lane];
+            __syncwarp();
+            int mycnt = 0;  // partners of home bubble h0 + lane so far
+            for (int w0 = 0; w0 < T; w0 += kTileChunks * 32) {
+                const int nch = min(kTileChunks, (T - w0 + 31) >> 5);
+                for (int ch = 0; ch < nch; ch++) {
+                    const int bb = w0 + (ch << 5) + lane;
+                    // the cell of candidate bb: the number of cells whose
+                    // inclusive prefix is <= bb (pre ascends over the lanes)
+                    int t = 0;
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1)
+                        if (__shfl_sync(kAll, pre, t + step - 1) <= bb) t += step;
+                    const int ct = __shfl_sync(kAll, cs, t), pt = __shfl_sync(kAll, pre, t),
+                              nt = __shfl_sync(kAll, cn, t), kt = __shfl_sync(kAll, key, t);
+                    int j = -1;
+                    // an unused lane tests a point far outside the box
+                    float4 pj = make_float4(1e18f, 1e18f, 1e18f, 0.f);
+                    if (bb < T) {
+                        j = ct + bb - (pt - nt);
+                        pj = pos[j];
+                        pj.x -= (kt & 1) ? L[0] : ((kt & 2) ? -L[0] : 0.f);
+                        pj.y -= (kt & 4) ? L[1] : ((kt & 8) ? -L[1] : 0.f);
+                        pj.z -= (kt & 16) ? L[2] : ((kt & 32) ? -L[2] : 0.f);
+                    }
+                    candj[w][(ch << 5) + lane] = j;
+                    const float wj = pj.w + skin;
+                    const bool amb = w0 + (ch << 5) < nhome  // home cell bubbles: only j > i
+                                         ? tile_tests<true>(home[w], nh, h0, j, pj, wj, tb,
+                                                            hitmask[w][ch])
+                                         : tile_tests<false>(home[w], nh, h0, j, pj, wj, tb,
+                                                             hitmask[w][ch]);
+                    if (amb)
+                        tile_exact<DIM>(k, home[w], nh, h0, j, pj, wj, tb, hitmask[w][ch], X,
+                                        Y, Z, R);
+                }
+                __syncwarp();
+                // each lane appends its home bubble's partners of the window
+                if (lane < nh) {
+                    int *row = stash + (size_t)(h0 + lane) * M;
+                    for (int ch = 0; ch < nch; ch++) {
+                        unsigned hm = hitmask[w][ch][lane];
+                        while (hm) {
+                            const int bit = __ffs(hm) - 1;
+                            hm &= hm - 1;
+                            if (mycnt < M) row[mycnt] = candj[w][(ch << 5) + bit];
+                            mycnt++;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+            if (lane < nh) {
+                const int i = h0 + lane;
+                NN[i] = mycnt;
+                rowCount[i] = mycnt;
+                over |= mycnt > M;
+            }
+        }
+    }
+    if (__syncthreads_or(over) && threadIdx.x == 0) atomicOr(&c->stash_over, 1);
+}
+CB_KERNEL_PAIR((template <int DIM>), k_pair_tiles, (<DIM>), __launch_bounds__(kBlock, 4))
 
 // The pair list from the counting pass's stash: row i's partners go to
 // rowStart[i] .. rowStart[i] + rowCount[i] (pairs grouped by i, j ascending
@@ -741,6 +956,7 @@ void launch_search(const Launch &l, const Bufs &b, int dim) {
         CB_LAUNCH(l, k_permute_a, (<3>), G, b);
         CB_LAUNCH(l, k_permute_b, (<3>), G, b);
         CB_LAUNCH(l, k_pair_cells, (<3, false>), G, b);
+        CB_LAUNCH(l, k_pair_tiles, (<3>), G, b);
         CB_LAUNCH(l, k_pair_rows, (<3>), G, b);
     } else {
         CB_LAUNCH(l, k_permute_a, (<2>), G, b);

@@ -136,7 +136,10 @@ CB_KERNEL_PAIR((template <int DIM>), k_predict, (<DIM>), __launch_bounds__(kBloc
 //     with (1/sqrt(m))^2; -w/4 on the exponent field; no product by f0 when
 //     it is 1;
 //   * contributions to both members go through FP64 reductions into the
-//     per-bubble accumulator rows.
+//     per-bubble accumulator rows;
+//   * overlap areas are accumulated in units of ov_unit (pi in 3D, 2 in 2D),
+//     one FP64 product less per overlapping pair; the unit is applied to the
+//     global sums and in the correct kernel.
 __device__ __forceinline__ void red_add(double *p, double v) {
     asm volatile("red.global.add.f64 [%0], %1;" ::"l"(p), "d"(v));
 }
@@ -152,6 +155,30 @@ __device__ __forceinline__ double neg_quarter(double w) {
 }
 
 constexpr int kQueue = 64;  // per-warp queue of overlapping pairs
+
+// Unit of the overlap rows the pair kernels write: pi in 3D (an overlap area
+// is pi (chord radius)^2), 2 in 2D (an overlap length is 2 (half chord)).
+__host__ __device__ constexpr double ov_unit(int dim) { return dim == 3 ? kPi : 2.0; }
+
+// The last block of a pair kernel: the attempt's total overlap area and
+// overlap area per radius (src/kernels.cu:264-267; each pair adds 2 A_overlap)
+// from the blocks' partial sums, which are in units of ov_unit, and the
+// mean-field factors of every bubble (src/kernels.cu:399-404).
+template <int DIM>
+__device__ __forceinline__ void pairs_fold(const Bufs &b, const int vb, const int vg,
+                                           double *smem) {
+    if (!last_block(&b.ctrl->done[DC_PAIRS], vg)) return;
+    const double fAo = fold_partials(b.part + 2 * vg, vg, false, smem);
+    const double fAor = fold_partials(b.part + 3 * vg, vg, false, smem);
+    if (threadIdx.x == 0) {
+        Ctrl *cc = b.ctrl;
+        cc->sumAo = (2.0 * ov_unit(DIM)) * fAo;
+        cc->sumAor = ov_unit(DIM) * fAor;
+        cc->mfa = (cc->sumAr - cc->sumAor) / (cc->sumA - cc->sumAo);
+        cc->mfb = b.k->kappa * b.k->ain * (double)cc->n / cc->sumA;
+        cc->done[DC_PAIRS] = 0;
+    }
+}
 
 // The overlap test of the reference in FP64 (the sign of the exact
 // (r1 + r2)^2 - m), for pairs in the FP32 guard band.
@@ -231,24 +258,15 @@ __device__ __forceinline__ void k_pairs_body(const Bufs &b, const int vb, const 
             }
             const bool inside = less_nonneg(m, r1sq) || less_nonneg(m, r2sq);
             // chord: r2^2 - t^2 / m with t = (r2^2 - r1^2 + m) / 2, as
-            // r2^2 - w^2 / 4 with w = (r2^2 - r1^2 + m) / |d|
+            // r2^2 - w^2 / 4 with w = (r2^2 - r1^2 + m) / |d|; the overlap
+            // area in units of ov_unit (pi in 3D, 2 in 2D)
             double oa;
-            if (DIM == 3) {
-                if (inside) {
-                    oa = min_nonneg(r1sq, r2sq);
-                } else {
-                    const double wv = (r2sq - r1sq + m) * rs;
-                    oa = abs_bits(fma(neg_quarter(wv), wv, r2sq));
-                }
-                oa *= kPi;
+            if (inside) {
+                oa = DIM == 3 ? min_nonneg(r1sq, r2sq) : min_nonneg(r1, r2);
             } else {
-                if (inside) {
-                    oa = 2.0 * min_nonneg(r1, r2);
-                } else {
-                    const double wv = (r2sq - r1sq + m) * rs;
-                    const double v = abs_bits(fma(neg_quarter(wv), wv, r2sq));
-                    oa = __double_as_longlong(v) > 0 ? 2.0 * (v * rsqrt_d(v)) : 0.0;
-                }
+                const double wv = (r2sq - r1sq + m) * rs;
+                oa = abs_bits(fma(neg_quarter(wv), wv, r2sq));
+                if (DIM == 2) oa = __double_as_longlong(oa) > 0 ? oa * rsqrt_d(oa) : 0.0;
             }
             const double g = oa * (inv2 - inv1);
             red_add(ai + 3, g);
@@ -342,19 +360,7 @@ __device__ __forceinline__ void k_pairs_body(const Bufs &b, const int vb, const 
         b.part[2 * vg + vb] = tAo;
         b.part[3 * vg + vb] = tAor;
     }
-    if (last_block(&b.ctrl->done[DC_PAIRS], vg)) {
-        const double fAo = fold_partials(b.part + 2 * vg, vg, false, smem);
-        const double fAor = fold_partials(b.part + 3 * vg, vg, false, smem);
-        if (threadIdx.x == 0) {
-            Ctrl *cc = b.ctrl;
-            cc->sumAo = 2.0 * fAo;  // each pair adds 2 A_overlap, :267
-            cc->sumAor = fAor;
-            // mean-field factors for every bubble, src/kernels.cu:399-404
-            cc->mfa = (cc->sumAr - cc->sumAor) / (cc->sumA - cc->sumAo);
-            cc->mfb = k.kappa * k.ain * (double)cc->n / cc->sumA;
-            cc->done[DC_PAIRS] = 0;
-        }
-    }
+    pairs_fold<DIM>(b, vb, vg, smem);
 }
 CB_KERNEL_PAIR((template <int DIM, bool GAS, bool FLOW>), k_pairs, (<DIM, GAS, FLOW>), __launch_bounds__(kBlock))
 
@@ -391,7 +397,6 @@ __device__ __forceinline__ void k_pairs_ff_body(const Bufs &b, const int vb, con
     const double *V0 = drow(b, c, RV0), *V1 = drow(b, c, RV1), *V2 = drow(b, c, RV2);
     const float4 *REC = b.ffr;
     const ff f0 = {k.f0_f, k.f0_l};
-    const ff pi = {(float)kPi, (float)(kPi - (double)(float)kPi)};
     const bool px = !k.wall[0], py = !k.wall[1], pz = DIM == 3 && !k.wall[2];
     const double hx = k.half_iv[0], hy = k.half_iv[1], hz = k.half_iv[2];
     const double Lx = k.iv[0], Ly = k.iv[1], Lz = k.iv[2];
@@ -498,17 +503,18 @@ __device__ __forceinline__ void k_pairs_ff_body(const Bufs &b, const int vb, con
             hit = true;
             if (GAS) {  // pairwise gas exchange, src/kernels.cu:236-280
                 // chord: r2^2 - t^2 / m with t = (r2^2 - r1^2 + m) / 2, as
-                // r2^2 - w^2 / 4 with w = (r2^2 - r1^2 + m) / |d|
+                // r2^2 - w^2 / 4 with w = (r2^2 - r1^2 + m) / |d|; the
+                // overlap area in units of ov_unit (pi in 3D, 2 in 2D)
                 ff oa;
                 if (inside) {
                     if (DIM == 3)
-                        oa = ff_mul(ff_less(ra.rsq, rb.rsq) ? ra.rsq : rb.rsq, pi);
+                        oa = ff_less(ra.rsq, rb.rsq) ? ra.rsq : rb.rsq;
                     else
-                        oa = ff_scale(ff_less(ra.r, rb.r) ? ra.r : rb.r, 2.f);
+                        oa = ff_less(ra.r, rb.r) ? ra.r : rb.r;
                 } else {
                     const ff w = ff_mul(ff_add(ff_sub(rb.rsq, ra.rsq), m), rs);
                     const ff v = ff_abs(ff_sub(rb.rsq, ff_scale(ff_sqr(w), 0.25f)));
-                    oa = DIM == 3 ? ff_mul(v, pi) : ff_scale(ff_sqrt(v), 2.f);
+                    oa = DIM == 3 ? v : ff_sqrt(v);
                 }
                 const ff gf = ff_mul(oa, ff_sub(rb.inv, ra.inv));
                 ag = ff_add(ag, gf);
@@ -533,19 +539,7 @@ __device__ __forceinline__ void k_pairs_ff_body(const Bufs &b, const int vb, con
         b.part[2 * vg + vb] = tAo;
         b.part[3 * vg + vb] = tAor;
     }
-    if (last_block(&b.ctrl->done[DC_PAIRS], vg)) {
-        const double fAo = fold_partials(b.part + 2 * vg, vg, false, smem);
-        const double fAor = fold_partials(b.part + 3 * vg, vg, false, smem);
-        if (threadIdx.x == 0) {
-            Ctrl *cc = b.ctrl;
-            cc->sumAo = 2.0 * fAo;  // each pair adds 2 A_overlap, :267
-            cc->sumAor = fAor;
-            // mean-field factors for every bubble, src/kernels.cu:399-404
-            cc->mfa = (cc->sumAr - cc->sumAor) / (cc->sumA - cc->sumAo);
-            cc->mfb = k.kappa * k.ain * (double)cc->n / cc->sumA;
-            cc->done[DC_PAIRS] = 0;
-        }
-    }
+    pairs_fold<DIM>(b, vb, vg, smem);
 }
 CB_KERNEL_PAIR((template <int DIM, bool GAS, bool FLOW>), k_pairs_ff, (<DIM, GAS, FLOW>), __launch_bounds__(kBlock, 3))
 
@@ -666,10 +660,12 @@ __device__ __forceinline__ void k_correct_body(const Bufs &b, const int vb, cons
     const double *PATH = drow(b, c, RPATH);
     double *PATHN = drow(b, c, RPATHN), *ERR = drow(b, c, RERR);
     const int *NN = irow(b, c, INN);
-    // mean-field factors, src/kernels.cu:399-408 (uniform over bubbles);
-    // area = 4 pi r^2 (3D) / 2 pi r (2D), so K / area = kq / r^2 (/ r)
+    // mean-field factors, src/kernels.cu:399-408 (uniform over bubbles).
+    // The overlap row ov and the pairwise rate are in units of ov_unit, and
+    // so is the area here: 4 r^2 (3D), pi r (2D); the unit goes into kq, the
+    // factor K ov_unit / area = kq / r^2 (/ r)
     const double mfa = c->mfa, mfb = c->mfb;
-    const double kq = DIM == 3 ? k.K * (0.25 / kPi) : k.K * (0.5 / kPi);
+    const double kq = DIM == 3 ? k.K * 0.25 : k.K * (1.0 / kPi);
     const double drag = 1.0 - k.wall_drag;
     long long merr = 0, mrad = 0, mexp = 0;
     double vol = 0.0;
@@ -717,10 +713,10 @@ __device__ __forceinline__ void k_correct_body(const Bufs &b, const int vb, cons
             if (DIM == 3) {  // (1/rp, rp^2) record of k_predict
                 const double2 e = reinterpret_cast<const double2 *>(b.invr)[i];
                 inv = e.x;
-                area = (4.0 * kPi) * e.y;
+                area = 4.0 * e.y;
             } else {
                 inv = p.w;
-                area = (2.0 * kPi) * rp;
+                area = kPi * rp;
             }
             double vr = mfa - inv;
             vr *= mfb * (area - ov);
@@ -756,7 +752,7 @@ __device__ __forceinline__ void k_correct_body(const Bufs &b, const int vb, cons
             P2[i] = vpz;
         }
         bad |= !(finite_bits(cx) && finite_bits(cy) && finite_bits(cz));
-        if (b.dbg_ov) b.dbg_ov[i] = ov;
+        if (b.dbg_ov) b.dbg_ov[i] = ov_unit(DIM) * ov;
         // leave the accumulators zeroed for the next attempt
         double4_32a zero;
         zero.x = zero.y = zero.z = zero.w = 0.0;

@@ -95,6 +95,37 @@ def test_search_rows_beyond_stash(oracle_mod, dim):
     int_rows_equal(g.get_state(), o.get_state())
 
 
+def test_search_dense_cluster_in_sparse_grid(oracle_mod):
+    """A 3D grid that is sparse on average (six cells per axis) with one
+    crowded spot: a large bubble in a shell of 300 small ones. The home cell
+    and its neighbours hold hundreds of bubbles, so the warp-per-cell
+    counting pass runs home blocks beyond 32 bubbles, candidate windows
+    beyond 512 and rows beyond the stash; the pair list is still the
+    oracle's, bit for bit, and the brute-force set."""
+    cfg, st = workloads.foam(2300, 3, 0.3, rmean=1.0, rstd=0.1, rclip=(0.5, 1.5), seed=108)
+    side = cfg.tfr[0]
+    rng = np.random.default_rng(109)
+    x, y, z, r = (np.array(st[k], dtype=np.float64) for k in ("x", "y", "z", "r"))
+    c = 0.5 * side
+    x[0] = y[0] = z[0] = c
+    r[0] = 2.5
+    d = rng.normal(size=(300, 3))
+    d *= (rng.uniform(0.5, 3.0, 300) / np.linalg.norm(d, axis=1))[:, None]
+    x[1:301], y[1:301], z[1:301] = c + d[:, 0], c + d[:, 1], c + d[:, 2]
+    r[1:301] = 0.3
+    st.update(x=x, y=y, z=z, r=r)
+    g, o = pair_both(oracle_mod, cfg, st)
+    g.search_neighbors()
+    o.search_neighbors()
+    gi, gj = g.pairs()
+    oi, oj = o.pairs()
+    assert np.bincount(oi, minlength=len(x)).max() > 32
+    assert np.array_equal(gi, oi) and np.array_equal(gj, oj)
+    sg = g.get_state()
+    int_rows_equal(sg, o.get_state())
+    assert set(zip(gi.tolist(), gj.tolist())) == brute_pairs(cfg, sg)
+
+
 @pytest.mark.parametrize("precision", [0, 2])
 @pytest.mark.parametrize("case", ["2d", "3d", "2d-wallx", "3d-wallz"])
 def test_bootstrap_and_attempt(oracle_mod, case, precision):
