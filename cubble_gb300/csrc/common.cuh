@@ -195,6 +195,19 @@ __device__ __forceinline__ int *irow(const Bufs &b, const Ctrl *c, int role) {
     return b.is[c->irole[role]];
 }
 
+// Row pointers of the correct kernels come from a per-block table in shared
+// memory, fetched at each use with a volatile load: a grid-stride loop would
+// otherwise keep all ~27 role-resolved 64-bit pointers in registers across
+// its iterations (mixed form, 3D: 119 registers and two blocks per SM; with
+// the table 64 registers and four blocks per SM).
+__device__ __forceinline__ void *tab_ptr(const unsigned long long *tab, int r) {
+    unsigned long long p;
+    asm volatile("ld.shared.u64 %0, [%1];"
+                 : "=l"(p)
+                 : "r"((unsigned int)__cvta_generic_to_shared(tab + r)));
+    return reinterpret_cast<void *>(p);
+}
+
 // Deterministic block reduction (fixed tree for a fixed blockDim).
 template <typename Op>
 __device__ __forceinline__ double block_reduce(double v, Op op, double *smem,

@@ -554,19 +554,6 @@ __device__ __forceinline__ bool touches_wall_f(float f0, float rad, float d1, fl
     return false;
 }
 
-// Row pointers of the correct kernel come from a per-block table in shared
-// memory, fetched at each use with a volatile load: a grid-stride loop would
-// otherwise keep all ~27 role-resolved 64-bit pointers in registers across
-// its iterations (119 registers in 3D, two blocks per SM; with the table
-// 64 registers and four blocks per SM).
-__device__ __forceinline__ void *tab_ptr(const unsigned long long *tab, int r) {
-    unsigned long long p;
-    asm volatile("ld.shared.u64 %0, [%1];"
-                 : "=l"(p)
-                 : "r"((unsigned int)__cvta_generic_to_shared(tab + r)));
-    return reinterpret_cast<void *>(p);
-}
-
 // One pass over the block for the correct kernel's five reductions: maxima of
 // error, radius and expansion (64-bit patterns of doubles >= 0), the volume
 // sum (FP64, fixed order for a fixed block size) and the deletion and
