@@ -125,10 +125,6 @@ __device__ __forceinline__ void k_wrap_body(const Bufs &b, const int vb, const i
         }
         mr = fmax(mr, R[i]);
     }
-    for (int q = vb * blockDim.x + threadIdx.x; q <= k.ccap; q += vg * blockDim.x) {
-        b.cellCount[q] = 0;
-        b.cellFill[q] = 0;
-    }
     const double t = __longlong_as_double(
         block_max_bits(__double_as_longlong(mr), reinterpret_cast<long long *>(smem)));
     if (threadIdx.x == 0) b.part[7 * vg + vb] = t;
@@ -186,12 +182,18 @@ CB_KERNEL_PAIR((), k_cell_fill, (), __launch_bounds__(kBlock))
 
 
 // One warp per cell: rank each member by its previous position (values are
-// distinct), giving the stable counting-sort order.
+// distinct), giving the stable counting-sort order. The cell's count and
+// fill counters are spent by now and are cleared here for the next search
+// (they start zeroed, and a search only touches its own ncell cells).
 __device__ __forceinline__ void k_cell_order_body(const Bufs &b, const int vb, const int vg) {
     const int ncell = b.ctrl->ncell;
     const int lane = threadIdx.x & 31;
     const int warps = vg * (blockDim.x >> 5);
     for (int q = vb * (blockDim.x >> 5) + (threadIdx.x >> 5); q < ncell; q += warps) {
+        if (lane == 0) {
+            b.cellCount[q] = 0;
+            b.cellFill[q] = 0;
+        }
         const int s = b.cellStart[q], e = b.cellStart[q + 1], m = e - s;
         for (int t0 = 0; t0 < m; t0 += 32) {
             const int t = t0 + lane;
@@ -223,53 +225,67 @@ __device__ __forceinline__ void gather_rate(const Bufs &b, const Ctrl *c, int fr
 }
 
 // Gather pass A: positions (+ saved), velocities, path, error, wrap counts
-// and indices into their spare slots, then swap the roles.
+// and indices into their spare slots, then swap the roles. One pass over
+// the bubbles: every row of a bubble is gathered in the same iteration (the
+// permutation read once, all loads of the bubble in flight together).
 template <int DIM>
 __device__ __forceinline__ void k_permute_a_body(const Bufs &b, const int vb, const int vg) {
     Ctrl *c = b.ctrl;
     const int n = c->n;
     const int *src = b.permSorted;
+    const bool f32 = b.k->mixed;  // rate rows hold floats in the mixed form
     const int roles[4][2] = {{RX, RXN}, {RY, RYN}, {RZ, RZN}, {RR, RRN}};
-    double *pos[4];
+    const double *pf[4];
+    double *pt[4], *sv[4];
+    const double *vf[4];
+    double *vt[4];
+#pragma unroll
     for (int a = 0; a < 4; a++) {
-        const double *from = drow(b, c, roles[a][0]);
-        double *to = drow(b, c, roles[a][1]);
-        double *sv = drow(b, c, RS0 + a);
-        pos[a] = to;
-        if (DIM == 2 && a == 2) continue;
-        for (int q = vb * blockDim.x + threadIdx.x; q < n; q += vg * blockDim.x) {
-            const double v = from[src[q]];
-            to[q] = v;
-            sv[q] = v;
-        }
+        pf[a] = drow(b, c, roles[a][0]);
+        pt[a] = drow(b, c, roles[a][1]);
+        sv[a] = drow(b, c, RS0 + a);
+        vf[a] = drow(b, c, RV0 + a);
+        vt[a] = drow(b, c, RVP0 + a);
     }
-    for (int a = 0; a < 4; a++) {
-        if (DIM == 2 && a == 2) continue;
-        gather_rate(b, c, RV0 + a, RVP0 + a, src, n, vb, vg);
-    }
-    {
-        const double *f1 = drow(b, c, RPATH), *f2 = drow(b, c, RERR);
-        double *t1 = drow(b, c, RPATHN), *t2 = drow(b, c, RERR2);
-        for (int q = vb * blockDim.x + threadIdx.x; q < n; q += vg * blockDim.x) {
-            const int s = src[q];
-            t1[q] = f1[s];
-            t2[q] = f2[s];
-        }
-    }
-    {
-        const int *f[4] = {irow(b, c, IWX), irow(b, c, IWY), irow(b, c, IWZ), irow(b, c, IIDX)};
-        int *t[4] = {irow(b, c, IWX2), irow(b, c, IWY2), irow(b, c, IWZ2), irow(b, c, IIDX2)};
-        for (int q = vb * blockDim.x + threadIdx.x; q < n; q += vg * blockDim.x) {
-            const int s = src[q];
-            t[0][q] = f[0][s];
-            t[1][q] = f[1][s];
-            t[2][q] = f[2][s];
-            t[3][q] = f[3][s];
-        }
-    }
+    const double *f1 = drow(b, c, RPATH), *f2 = drow(b, c, RERR);
+    double *t1 = drow(b, c, RPATHN), *t2 = drow(b, c, RERR2);
+    const int *fi[4] = {irow(b, c, IWX), irow(b, c, IWY), irow(b, c, IWZ), irow(b, c, IIDX)};
+    int *ti[4] = {irow(b, c, IWX2), irow(b, c, IWY2), irow(b, c, IWZ2), irow(b, c, IIDX2)};
     for (int q = vb * blockDim.x + threadIdx.x; q < n; q += vg * blockDim.x) {
-        b.pos32[q] = make_float4((float)pos[0][q], (float)pos[1][q],
-                                 DIM == 3 ? (float)pos[2][q] : 0.0f, (float)pos[3][q]);
+        const int s = src[q];
+        double p[4];
+#pragma unroll
+        for (int a = 0; a < 4; a++) p[a] = (DIM == 2 && a == 2) ? 0.0 : pf[a][s];
+        double v[4];
+        float vf32[4];
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            if (DIM == 2 && a == 2) continue;
+            if (f32)
+                vf32[a] = reinterpret_cast<const float *>(vf[a])[s];
+            else
+                v[a] = vf[a][s];
+        }
+        const double g1 = f1[s], g2 = f2[s];
+        const int w0 = fi[0][s], w1 = fi[1][s], w2 = fi[2][s], w3 = fi[3][s];
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            if (DIM == 2 && a == 2) continue;
+            pt[a][q] = p[a];
+            sv[a][q] = p[a];
+            if (f32)
+                reinterpret_cast<float *>(vt[a])[q] = vf32[a];
+            else
+                vt[a][q] = v[a];
+        }
+        t1[q] = g1;
+        t2[q] = g2;
+        ti[0][q] = w0;
+        ti[1][q] = w1;
+        ti[2][q] = w2;
+        ti[3][q] = w3;
+        b.pos32[q] = make_float4((float)p[0], (float)p[1], DIM == 3 ? (float)p[2] : 0.0f,
+                                 (float)p[3]);
     }
     if (last_block(&c->done[DC_PERMUTE], vg) && threadIdx.x == 0) {
         int *r = c->drole;
