@@ -29,7 +29,8 @@ def load_prepared(f, st):
 
 def displacement_err(cfg, s_a, s_b, s0):
     err = 0.0
-    for a, k in enumerate(("x", "y")):
+    axes = ("x", "y", "z") if cfg.dimensionality == 3 else ("x", "y")
+    for a, k in enumerate(axes):
         L = cfg.tfr[a] - cfg.lbb[a]
         d = s_a[k] - s_b[k]
         d = d - L * np.round(d / L)
@@ -72,6 +73,26 @@ def compare_with_single(items, precision, graph, steps, tol):
 def test_batch_mixed_matches_single(graph):
     n = compare_with_single(small_sweep(precision=1, graph=graph), 1, graph, 40, 1e-6)
     assert n > 0
+
+
+def foams_3d(precision, walls, graph=1):
+    """3D foams of uneven sizes (six or more cells per periodic axis: the
+    search's counting pass is the warp-per-cell one), periodic or all with
+    walls in z (a batch holds foams of one wall presence)."""
+    wall = (0, 0, 1) if walls else (0, 0, 0)
+    return [workloads.foam(n, 3, 0.8, rstd=0.15, rclip=(0.3, 2.5), seed=70 + f, wall=wall,
+                           wall_drag=0.1 if walls else 0.0, precision=precision,
+                           use_graph=graph)
+            for f, n in enumerate((6000, 11000, 3500))]
+
+
+@pytest.mark.parametrize("walls", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_3d_matches_single(precision, walls):
+    """3D foams batched and alone: the batched forms of the 3D search and
+    attempt kernels on virtual grids."""
+    tol = 1e-12 if precision == 0 else 1e-6
+    compare_with_single(foams_3d(precision, walls), precision, 1, 30, tol)
 
 
 def test_batch_fp64_matches_single():
