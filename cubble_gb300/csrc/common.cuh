@@ -82,6 +82,7 @@ struct DevConst {
     int ffpair;  // CB_PRECISION_FP64_FF: pair terms in float-float
     float kq_f;  // K / (4 pi) in 3D, K / (2 pi) in 2D, as FP32
     float pre_margin;  // FP32 pair-search prefilter margin (length units)
+    long long lbq[3];  // the box's lower corner in fixed point (x 2^40)
     float half_iv32[3];
     float iv32[3];
     // Linear shear flow (cb_config.shear_speed): v_x += shear (2 (q - lbb_q)
@@ -178,6 +179,7 @@ struct Bufs {
     int *rowCount;      // cap + 1
     int *rowStart;      // cap + 1
     float4 *pos32;      // FP32 copy of x, y, z, r for the search prefilter
+    float4 *pos32r;     // the same with x, y, z relative to the bubble's cell (3D tile pass)
     int *holes;         // cap
     int *moveDst;       // cap
     int *keep;          // pcap + 1
@@ -193,6 +195,33 @@ __device__ __forceinline__ double *drow(const Bufs &b, const Ctrl *c, int role) 
 }
 __device__ __forceinline__ int *irow(const Bufs &b, const Ctrl *c, int role) {
     return b.is[c->irole[role]];
+}
+
+// 64-bit fixed point x * 2^40 (the mixed form's predicted positions, the
+// search's cell-relative coordinates), converted on the integer pipe: GB300
+// runs every 64-bit conversion on its 1/64-rate FP64 unit.
+constexpr int kFixBits = 40;
+constexpr float kFixInv = 9.094947017729282e-13f;  // 2^-40
+
+// x * 2^40 rounded toward zero, from the bits of x (|x| < 2^23).
+__device__ __forceinline__ long long fix_from_double(double x) {
+    const long long b = __double_as_longlong(x);
+    const int e = (int)(((unsigned long long)b >> 52) & 0x7ff);
+    const long long m = (b & 0x000fffffffffffffLL) | 0x0010000000000000LL;
+    const int sh = e - (1075 - kFixBits);  // x = m 2^(e - 1075)
+    long long q = sh >= 0 ? (m << min(sh, 10)) : (sh > -64 ? (m >> -sh) : 0LL);
+    if (e == 0) q = 0;
+    return b < 0 ? -q : q;
+}
+
+// A fixed-point difference in length units as FP32: |d| = hi 2^32 + lo with
+// two 32-bit conversions (the 64-bit one would take the FP64 unit); relative
+// error below 2^-23.
+__device__ __forceinline__ float len_from_fix(long long d) {
+    const unsigned long long a = (unsigned long long)(d < 0 ? -d : d);
+    const float f = fmaf(__uint2float_rn((unsigned int)(a >> 32)), 4294967296.f,
+                         __uint2float_rn((unsigned int)a));
+    return (d < 0 ? -f : f) * kFixInv;
 }
 
 // Row pointers of the correct kernels come from a per-block table in shared

@@ -90,6 +90,7 @@ void fill_const(cb_context *c) {
     for (int a = 0; a < 3; a++) {
         k.lq[a] = (long long)std::llround(k.iv[a] * 1099511627776.0);  // 2^40
         k.hq[a] = k.lq[a] / 2;
+        k.lbq[a] = (long long)std::llround(k.lbb[a] * 1099511627776.0);
     }
     // Guard band of the FP32 pair prefilters. An FP32 coordinate carries up
     // to 2^-24 |x| rounding, a periodic shift or minimum image another
@@ -456,6 +457,7 @@ int cbg::create_context(const cb_config *cfg, cb_context **out, bool graph) {
     if ((rc = c->alloc(&b.rowCount, cap + 1))) return bail(rc);
     if ((rc = c->alloc(&b.rowStart, cap + 1))) return bail(rc);
     if ((rc = c->alloc(&b.pos32, cap))) return bail(rc);
+    if (c->hk.dim == 3 && (rc = c->alloc(&b.pos32r, cap))) return bail(rc);
     if ((rc = c->alloc(&b.holes, cap))) return bail(rc);
     if ((rc = c->alloc(&b.moveDst, cap))) return bail(rc);
     if ((rc = c->alloc(&b.keep, pcap + 1))) return bail(rc);

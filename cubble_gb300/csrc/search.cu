@@ -224,6 +224,17 @@ __device__ __forceinline__ void gather_rate(const Bufs &b, const Ctrl *c, int fr
     }
 }
 
+// Sparse 3D grids whose periodic axes have at least four cells (and fewer
+// than 2^26 cells) are counted by k_pair_tiles: a neighbour cell is then
+// reached through at most one periodic image, and never twice.
+template <int DIM>
+__device__ __forceinline__ bool tile_grid(const DevConst &k, const int cd[3], int ncell) {
+    bool ok = DIM == 3 && ncell < (1 << 26);  // cell index and stencil offset in one sort key
+#pragma unroll
+    for (int a = 0; a < DIM; a++) ok &= k.wall[a] || cd[a] >= 4;
+    return ok;
+}
+
 // Gather pass A: positions (+ saved), velocities, path, error, wrap counts
 // and indices into their spare slots, then swap the roles. One pass over
 // the bubbles: every row of a bubble is gathered in the same iteration (the
@@ -251,6 +262,18 @@ __device__ __forceinline__ void k_permute_a_body(const Bufs &b, const int vb, co
     double *t1 = drow(b, c, RPATHN), *t2 = drow(b, c, RERR2);
     const int *fi[4] = {irow(b, c, IWX), irow(b, c, IWY), irow(b, c, IWZ), irow(b, c, IIDX)};
     int *ti[4] = {irow(b, c, IWX2), irow(b, c, IWY2), irow(b, c, IWZ2), irow(b, c, IIDX2)};
+    // for the 3D tile pass: x, y, z relative to the lower corner of the
+    // bubble's cell, from exact fixed-point differences (x 2^40; the cell
+    // edge L / cd in that unit, off by at most one unit)
+    const DevConst &k = *b.k;
+    const int cd[3] = {c->cell_dims[0], c->cell_dims[1], c->cell_dims[2]};
+    const bool rel = DIM == 3 && c->sparse_cells && tile_grid<DIM>(k, cd, c->ncell);
+    long long cwq[3], lbq[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        cwq[a] = k.lq[a] / cd[a];
+        lbq[a] = k.lbq[a];
+    }
     for (int q = vb * blockDim.x + threadIdx.x; q < n; q += vg * blockDim.x) {
         const int s = src[q];
         double p[4];
@@ -286,6 +309,15 @@ __device__ __forceinline__ void k_permute_a_body(const Bufs &b, const int vb, co
         ti[3][q] = w3;
         b.pos32[q] = make_float4((float)p[0], (float)p[1], DIM == 3 ? (float)p[2] : 0.0f,
                                  (float)p[3]);
+        if (rel) {
+            const int cell = b.cellSorted[q];
+            const int kc[3] = {cell % cd[0], (cell / cd[0]) % cd[1], cell / (cd[0] * cd[1])};
+            float o[3];
+#pragma unroll
+            for (int a = 0; a < 3; a++)
+                o[a] = len_from_fix(fix_from_double(p[a]) - (lbq[a] + (long long)kc[a] * cwq[a]));
+            b.pos32r[q] = make_float4(o[0], o[1], o[2], (float)p[3]);
+        }
     }
     if (last_block(&c->done[DC_PERMUTE], vg) && threadIdx.x == 0) {
         int *r = c->drole;
@@ -387,25 +419,6 @@ static __device__ __noinline__ bool pair_take_exact(const DevConst &k, int i, in
     const double sq = exact_sqdist<DIM>(k, X[i], Y[i], DIM == 3 ? Z[i] : 0.0, X[j], Y[j],
                                         DIM == 3 ? Z[j] : 0.0);
     return sq < __dmul_rn(maxd, maxd);
-}
-// pair_class on a difference that needs no minimum image: `ps` is the
-// bubble's position already moved by the periodic image shift of the
-// candidate's cell.
-template <int DIM>
-__device__ __forceinline__ int pair_class_direct(const DevConst &k, const float4 &ps,
-                                                 const float4 &pj) {
-    const float dx = ps.x - pj.x, dy = ps.y - pj.y;
-    float d2 = fmaf(dx, dx, dy * dy);
-    if (DIM == 3) {
-        const float dz = ps.z - pj.z;
-        d2 = fmaf(dz, dz, d2);
-    }
-    const float cut = ps.w + pj.w + k.skin_f;
-    const float band = k.pre_margin;
-    const float hi = cut + band, lo = fmaxf(cut - band, 0.f);
-    if (d2 >= hi * hi) return 0;
-    if (d2 < lo * lo) return 1;
-    return 2;
 }
 // The FP32 part of the test: 0 not a partner, 1 a partner, 2 within the
 // guard band (the exact test decides).
@@ -529,17 +542,6 @@ __device__ __forceinline__ void k_pair_cells_body(const Bufs &b, const int vb, c
 }
 CB_KERNEL_PAIR((template <int DIM, bool WRITE>), k_pair_cells, (<DIM, WRITE>), __launch_bounds__(kBlock))
 
-// Sparse 3D grids whose periodic axes have at least four cells (and fewer
-// than 2^25 cells) are counted by k_pair_tiles: a neighbour cell is then
-// reached through at most one periodic image, and never twice.
-template <int DIM>
-__device__ __forceinline__ bool tile_grid(const DevConst &k, const int cd[3], int ncell) {
-    bool ok = DIM == 3 && ncell < (1 << 25);  // cell index and shift in one sort key
-#pragma unroll
-    for (int a = 0; a < DIM; a++) ok &= k.wall[a] || cd[a] >= 4;
-    return ok;
-}
-
 // Counting pass for sparse 2D cell grids (fewer than 24 bubbles per cell on
 // average; 2D cells hold ~3) and the sparse 3D grids k_pair_tiles does not
 // take (an axis with fewer than four cells): one thread per bubble walks its
@@ -659,9 +661,13 @@ CB_KERNEL_PAIR((template <int DIM>), k_pair_rows, (<DIM>), __launch_bounds__(kBl
 // bubbles and those of its neighbour cells >= it, cells ascending, bubbles
 // ascending inside a cell) are laid over the lanes 32 at a time, each lane
 // loading one candidate (a cell's bubbles are contiguous, so the loads are
-// coalesced) and moving it by its cell's periodic image shift into the home
-// cell's frame (four or more cells per axis make the shift unique, and
-// candidates are tested on plain differences). The home cell's bubbles are
+// coalesced). Coordinates are FP32 relative to each bubble's cell corner
+// (written by the gather into cell order from exact fixed-point
+// differences), and a candidate moves into the home cell's frame by its
+// cell's stencil offset times the cell edge, across a periodic face too
+// (four or more cells per axis make the offset unique): the FP32 rounding
+// is relative to a cell edge, not to the box, and the guard band where the
+// reference's FP64 test decides is ~50x narrower. The home cell's bubbles are
 // then broadcast from shared memory one at a time and every lane tests its
 // candidate against the bubble; the warp's hit mask of each (bubble, chunk)
 // goes to shared memory, and after a window of up to kTileChunks chunks each
@@ -683,7 +689,7 @@ template <bool CMP>
 __device__ __forceinline__ bool tile_tests(const float4 *home, int nh, int h0, int j,
                                            const float4 &pj, float wj, float tb,
                                            unsigned *masks) {
-    unsigned amb_any = 0;
+    float bmin = 3.4e38f;  // min over the home bubbles of |e| (<= tb: in the band)
 #pragma unroll 4
     for (int a = 0; a < nh; a++) {
         const float4 pi = home[a];
@@ -691,25 +697,22 @@ __device__ __forceinline__ bool tile_tests(const float4 *home, int nh, int h0, i
         const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
         const float cut = pi.w + wj;
         const float e = fmaf(-cut, cut, d2);
-        bool take = e < -tb, amb = e < tb;
-        if (CMP) {
-            take &= j > h0 + a;
-            amb &= j > h0 + a;
-        }
+        bool take = e < -tb;
+        if (CMP) take &= j > h0 + a;
         masks[a] = __ballot_sync(0xffffffffu, take);
-        amb_any |= __ballot_sync(0xffffffffu, amb && !take);
+        bmin = fminf(bmin, fabsf(e));
     }
-    return amb_any != 0;
+    return __any_sync(0xffffffffu, bmin <= tb);
 }
 // The FP64 test of the reference for the guard-band pairs of a chunk: the
 // chunk's tests are repeated and each band pair's bit set by the exact
-// decision (comparePair, src/kernels.cu:619-623).
+// decision (comparePair, src/kernels.cu:619-623). Rare: with the
+// cell-relative band about one chunk in 1500 at N = 10^6.
 template <int DIM>
-static __device__ __noinline__ void tile_exact(const DevConst &k, const float4 *home, int nh,
-                                               int h0, int j, float4 pj, float wj, float tb,
-                                               unsigned *masks, const double *X,
-                                               const double *Y, const double *Z,
-                                               const double *R) {
+__device__ __forceinline__ void tile_exact(const DevConst &k, const float4 *home, int nh, int h0,
+                                           int j, float4 pj, float wj, float tb, unsigned *masks,
+                                           const double *X, const double *Y, const double *Z,
+                                           const double *R) {
     const int lane = threadIdx.x & 31;
     __syncwarp();
     for (int a = 0; a < nh; a++) {
@@ -743,12 +746,25 @@ __device__ __forceinline__ void k_pair_tiles_body(const Bufs &b, const int vb, c
     int *NN = irow(b, c, INN);
     int *stash = b.stash, *rowCount = b.rowCount;
     const int *cellStart = b.cellStart;
-    const float4 *pos = b.pos32;
+    const float4 *pos = b.pos32r;  // x, y, z relative to the bubble's cell
     // constants in registers (a store through `stash` could alias them)
-    // the guard band in d2 - cut^2 units: 2 cut band for the largest cut
     const float skin = k.skin_f;
-    const float tb = 2.f * k.pre_margin * (2.f * (c->search_maxr + 1e-3f) + skin);
-    const float L[3] = {k.iv32[0], k.iv32[1], k.iv32[2]};
+    // cell edges (the unit of the fixed-point cell corners, rounded to FP32)
+    float cw[3], cwmax = 0.f;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        cw[a] = (float)(k.lq[a] / cd[a]) * kFixInv;
+        cwmax = fmaxf(cwmax, cw[a]);
+    }
+    // Guard band of the cell-relative FP32 test. A coordinate relative to
+    // its cell's corner is off by < 2^-23 cw (its conversion), the cell
+    // offset of a candidate by 2^-24 cw, the moved candidate (|x| < 2 cw)
+    // and the difference by 2^-24 2 cw each: < 8 2^-24 cw per axis, so the
+    // distance by < 8.3e-7 cw; the squared-distance and cutoff roundings add
+    // < 1e-6. 4e-6 cw + 2e-6 is about 4x that. In d2 - cut^2 units: 2 cut
+    // band for the largest cut.
+    const float band = 4e-6f * cwmax + 2e-6f;
+    const float tb = 2.f * band * (2.f * (c->search_maxr + 1e-3f) + skin);
     const bool per[3] = {!k.wall[0], !k.wall[1], !k.wall[2]};
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int plane = cd[0] * cd[1];
@@ -758,11 +774,11 @@ __device__ __forceinline__ void k_pair_tiles_body(const Bufs &b, const int vb, c
         const int s0 = cellStart[cell], e0 = cellStart[cell + 1];
         if (s0 == e0) continue;
         // lane t < m: the t-th neighbour cell >= cell in ascending order
-        // (getNeighborCellIndex, src/kernels.cu:1157-1189) with its periodic
-        // image shift in the low 6 bits of the key (2 bits per axis: 1 =
-        // reached below 0, the candidate is moved by -L; 2 = reached above
-        // the box, moved by +L). Away from the box faces these are the
-        // offsets 13..26 of the 27-cell stencil in order, with no shift.
+        // (getNeighborCellIndex, src/kernels.cu:1157-1189) with its stencil
+        // offset o (0..26: (o % 3 - 1, o / 3 % 3 - 1, o / 9 - 1) cells) in
+        // the low 5 bits of the key: a candidate moves into the home cell's
+        // frame by the offset times the cell edge, across a periodic face
+        // too. Away from the box faces these are the offsets 13..26 in order.
         const int hk[3] = {cell % cd[0], (cell / cd[0]) % cd[1], cell / plane};
         const bool inner = hk[0] >= 1 && hk[0] <= cd[0] - 2 && hk[1] >= 1 &&
                            hk[1] <= cd[1] - 2 && hk[2] >= 1 && hk[2] <= cd[2] - 2;
@@ -770,37 +786,30 @@ __device__ __forceinline__ void k_pair_tiles_body(const Bufs &b, const int vb, c
         if (inner) {
             if (lane < 14) {
                 const int o = 13 + lane;
-                key = (cell + (o / 9 - 1) * plane + ((o / 3) % 3 - 1) * cd[0] + (o % 3 - 1)) << 6;
+                key = ((cell + (o / 9 - 1) * plane + ((o / 3) % 3 - 1) * cd[0] + (o % 3 - 1)) << 5) | o;
             }
         } else {
             if (lane < 27) {
                 const int off[3] = {lane % 3 - 1, (lane / 3) % 3 - 1, lane / 9 - 1};
-                int q[3], sh = 0;
+                int q[3];
                 bool ok = true;
 #pragma unroll
                 for (int a = 0; a < 3; a++) {
                     q[a] = hk[a] + off[a];
-                    if (per[a]) {
-                        if (q[a] < 0) {
-                            q[a] += cd[a];
-                            sh |= 1 << (2 * a);
-                        } else if (q[a] >= cd[a]) {
-                            q[a] -= cd[a];
-                            sh |= 2 << (2 * a);
-                        }
-                    } else {
+                    if (per[a])
+                        q[a] = q[a] < 0 ? q[a] + cd[a] : (q[a] >= cd[a] ? q[a] - cd[a] : q[a]);
+                    else
                         ok &= q[a] >= 0 && q[a] < cd[a];
-                    }
                 }
                 const int v = (q[2] * cd[1] + q[1]) * cd[0] + q[0];
-                if (ok && v >= cell) key = (v << 6) | sh;
+                if (ok && v >= cell) key = (v << 5) | lane;
             }
             key = warp_sort(key);
             m = __popc(__ballot_sync(kAll, key != 0x7fffffff));
         }
         int cs = 0, cn = 0;
         if (lane < m) {
-            const int v = key >> 6;
+            const int v = key >> 5;
             cs = cellStart[v];
             cn = cellStart[v + 1] - cs;
         }
@@ -836,9 +845,10 @@ __device__ __forceinline__ void k_pair_tiles_body(const Bufs &b, const int vb, c
                     if (bb < T) {
                         j = ct + bb - (pt - nt);
                         pj = pos[j];
-                        pj.x -= (kt & 1) ? L[0] : ((kt & 2) ? -L[0] : 0.f);
-                        pj.y -= (kt & 4) ? L[1] : ((kt & 8) ? -L[1] : 0.f);
-                        pj.z -= (kt & 16) ? L[2] : ((kt & 32) ? -L[2] : 0.f);
+                        const int o = kt & 31;
+                        pj.x = fmaf((float)(o % 3 - 1), cw[0], pj.x);
+                        pj.y = fmaf((float)((o / 3) % 3 - 1), cw[1], pj.y);
+                        pj.z = fmaf((float)(o / 9 - 1), cw[2], pj.z);
                     }
                     candj[w][(ch << 5) + lane] = j;
                     const float wj = pj.w + skin;

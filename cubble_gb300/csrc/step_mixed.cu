@@ -31,25 +31,12 @@
 namespace cbg {
 namespace {
 
-constexpr int kFixBits = 40;
-constexpr float kFixInv = 9.094947017729282e-13f;  // 2^-40
-
 __device__ __forceinline__ float *frow(const Bufs &b, const Ctrl *c, int role) {
     return reinterpret_cast<float *>(b.ds[c->drole[role]]);
 }
 
 // ------------------------------------------------- integer-pipe conversions
-// x * 2^40 rounded toward zero, from the bits of x (|x| < 2^23).
-__device__ __forceinline__ long long fix_from_double(double x) {
-    const long long b = __double_as_longlong(x);
-    const int e = (int)(((unsigned long long)b >> 52) & 0x7ff);
-    const long long m = (b & 0x000fffffffffffffLL) | 0x0010000000000000LL;
-    const int sh = e - (1075 - kFixBits);  // x = m 2^(e - 1075)
-    long long q = sh >= 0 ? (m << min(sh, 10)) : (sh > -64 ? (m >> -sh) : 0LL);
-    if (e == 0) q = 0;
-    return b < 0 ? -q : q;
-}
-
+// (fix_from_double and len_from_fix are in common.cuh)
 // f * 2^40 rounded toward zero, from the bits of f (|f| < 2^23).
 __device__ __forceinline__ long long fix_from_float(float f) {
     const int b = __float_as_int(f);
@@ -59,15 +46,6 @@ __device__ __forceinline__ long long fix_from_float(float f) {
     long long q = sh >= 0 ? (m << min(sh, 39)) : (sh > -64 ? (m >> -sh) : 0LL);
     if (e == 0) q = 0;
     return b < 0 ? -q : q;
-}
-
-// A fixed-point difference in length units as FP32: |d| = hi 2^32 + lo with
-// two 32-bit conversions (the 64-bit one would take the FP64 unit).
-__device__ __forceinline__ float len_from_fix(long long d) {
-    const unsigned long long a = (unsigned long long)(d < 0 ? -d : d);
-    const float f = fmaf(__uint2float_rn((unsigned int)(a >> 32)), 4294967296.f,
-                         __uint2float_rn((unsigned int)a));
-    return (d < 0 ? -f : f) * kFixInv;
 }
 
 // Exact float -> double from the bits (FP32 subnormals become 0).
