@@ -336,7 +336,7 @@ __device__ __forceinline__ void k_permute_a_body(const Bufs &b, const int vb, co
         c->done[DC_PERMUTE] = 0;
     }
 }
-CB_KERNEL_PAIR((template <int DIM>), k_permute_a, (<DIM>), __launch_bounds__(kBlock))
+CB_KERNEL_PAIR((template <int DIM>), k_permute_a, (<DIM>), __launch_bounds__(kBlock, 4))
 
 
 // Gather pass B: previous velocities into the slot the old velocities left.
