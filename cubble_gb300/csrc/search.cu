@@ -91,6 +91,23 @@ __device__ __forceinline__ int cell_coord_fast(double x, const CellAxis &c) {
     return cell_coord_slow(x, c.lbb_d, c.iv, c.cd);
 }
 
+__device__ __forceinline__ bool is_nan_bits(double x) {
+    return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+}
+// A double's bit pattern as a signed integer that orders like the value
+// (-0 and +0 both 0; NaN patterns beyond the infinities).
+__device__ __forceinline__ long long order_key(double x) {
+    const long long b = __double_as_longlong(x);
+    return b >= 0 ? b : (long long)(0x8000000000000000ULL - (unsigned long long)b);
+}
+// The wrap itself (rare): x + (hi - lo) mult and the wrap count, a call so
+// that its FP64 arithmetic is not predicated into every bubble.
+static __device__ __noinline__ void wrap_one(double *xp, int *wp, double x, double lo, double hi,
+                                             int mult) {
+    *xp = x + (hi - lo) * (double)mult;
+    *wp -= mult;
+}
+
 template <int DIM>
 __device__ __forceinline__ void k_wrap_body(const Bufs &b, const int vb, const int vg) {
     __shared__ double smem[32];
@@ -101,32 +118,33 @@ __device__ __forceinline__ void k_wrap_body(const Bufs &b, const int vb, const i
     int *WR[3] = {irow(b, c, IWX), irow(b, c, IWY), irow(b, c, IWZ)};
     const double *R = drow(b, c, RR);
     // box constants in registers: the stores below may alias them for the
-    // compiler, which would reload them per bubble
+    // compiler, which would reload them per bubble. The compares of
+    // wrapOverPeriodicBoundaries (src/kernels.cu:992-1011) run on the integer
+    // pipe, on order keys of the bit patterns (-0 and +0 alike; a NaN
+    // coordinate is left alone and a NaN radius ignored, as the FP64
+    // compares and fmax do).
     bool per[3];
-    double lo3[3], hi3[3];
+    long long lo3[3], hi3[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         per[a] = a < DIM && !k.wall[a];
-        lo3[a] = k.lbb[a];
-        hi3[a] = k.tfr[a];
+        lo3[a] = order_key(k.lbb[a]);
+        hi3[a] = order_key(k.tfr[a]);
     }
-    double mr = 0.0;
+    long long mr = 0;  // largest radius as the bits of a double >= 0
     for (int i = vb * blockDim.x + threadIdx.x; i < n; i += vg * blockDim.x) {
 #pragma unroll
         for (int a = 0; a < DIM; a++) {
             if (!per[a]) continue;
-            const double lo = lo3[a], hi = hi3[a];
             const double x = XR[a][i];
-            const int mult = x < lo ? 1 : (x > hi ? -1 : 0);
-            if (mult) {
-                XR[a][i] = x + (hi - lo) * (double)mult;
-                WR[a][i] -= mult;
-            }
+            const long long kx = order_key(x);
+            const int mult = is_nan_bits(x) ? 0 : (kx < lo3[a] ? 1 : (kx > hi3[a] ? -1 : 0));
+            if (mult) wrap_one(XR[a] + i, WR[a] + i, x, k.lbb[a], k.tfr[a], mult);
         }
-        mr = fmax(mr, R[i]);
+        const double r = R[i];
+        if (!is_nan_bits(r)) mr = max(mr, __double_as_longlong(r));  // fmax over radii >= 0
     }
-    const double t = __longlong_as_double(
-        block_max_bits(__double_as_longlong(mr), reinterpret_cast<long long *>(smem)));
+    const double t = __longlong_as_double(block_max_bits(mr, reinterpret_cast<long long *>(smem)));
     if (threadIdx.x == 0) b.part[7 * vg + vb] = t;
     if (last_block(&c->done[DC_WRAP], vg)) {
         const double f = fold_partials(b.part + 7 * vg, vg, true, smem);
