@@ -454,8 +454,9 @@ void init_previous(Run &r) {
 }
 
 // ------------------------------------------------------------ checkpoint
-// The complete AB2 state, the pair list, the clock and the driver's host
-// data, so that a resumed run continues step for step. Not in the reference.
+// The complete AB2 state, the pair list, the clock and the simulation
+// loop's host data, so that a resumed run continues step for step. Not in
+// the reference.
 constexpr char kMagic[8] = {'C', 'B', 'G', 'C', 'K', 'P', 'T', '1'};
 
 template <typename T>

@@ -1,4 +1,4 @@
-"""TEST INFRASTRUCTURE and BASELINE: runs the REFERENCE's own device code.
+"""TEST INFRASTRUCTURE and reference timing: runs the REFERENCE's own device code.
 
 KJLankinen/cubble's src/kernels.cu, compiled unmodified by
 oracle/ref/build_ref.py into oracle/_ref/kernels_ref.cubin, is loaded on the

@@ -24,7 +24,7 @@ and 3D, and the 2D N = 10^4 configuration):
 With --init it writes init_2d.npz / init_3d.npz instead: init()'s
 assignDataToBubbles on seeded draws and transformPositions both ways.
 
-Run on the GPU machine (torch provides the device buffers, ctypes the driver API):
+Run on a GB300 (torch provides the device buffers, ctypes the CUDA driver API):
     python tests/golden/make_golden.py [--init] [--only=NAME,...] OUT_DIR
 (OUT_DIR is required; --only records just the named cases). The .npz files
 it writes are committed under tests/golden/.

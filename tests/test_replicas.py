@@ -4,7 +4,7 @@ foam) with the gloo backend and two ranks on 127.0.0.1.
   * the rank helpers: process-group set-up from the torchrun environment, the
     barrier, and the reductions the line uses (sum of bubble-steps over ranks,
     maximum of the timed region);
-  * the reference arm launched like the driver launches it for N = 2: rank 0
+  * the reference arm launched through torchrun for N = 2: rank 0
     alone runs the CPU restatement and prints one JSON line, rank 1 exits 0
     without work.
 """
