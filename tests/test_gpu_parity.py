@@ -95,6 +95,36 @@ def test_search_rows_beyond_stash(oracle_mod, dim):
     int_rows_equal(g.get_state(), o.get_state())
 
 
+@pytest.mark.parametrize("cells", [3, 4])
+def test_search_thin_periodic_box(oracle_mod, cells):
+    """A 3D periodic box with only 3 or 4 cells along x (9 along y and z):
+    at 4 the warp-per-cell counting pass takes it (every stencil offset a
+    distinct cell, one periodic image each), at 3 the thread-per-bubble pass
+    with the minimum image. Pair list bit-exact against the oracle and equal
+    to the brute-force set."""
+    rng = np.random.default_rng(110 + cells)
+    r = np.clip(rng.normal(1.0, 0.1, 4000), 0.5, 1.3)
+    r[0] = 1.3  # the largest radius, whatever the sample size below
+    cut = 2.0 * r.max() + 0.3
+    lx, ly = (cells + 0.5) * cut, 9.5 * cut
+    n = int(0.8 * lx * ly * ly / (4.0 / 3.0 * math.pi * float(np.mean(r ** 3))))
+    r = r[:n]
+    cfg, st = workloads.foam(n, 3, 0.8, seed=110 + cells, rclip=(0.5, 1.3))
+    cfg.tfr[0], cfg.tfr[1], cfg.tfr[2] = lx, ly, ly
+    st = {"x": rng.uniform(0.0, lx, n), "y": rng.uniform(0.0, ly, n),
+          "z": rng.uniform(0.0, ly, n), "r": r, "index": np.arange(n, dtype=np.int32)}
+    g, o = pair_both(oracle_mod, cfg, st)
+    g.search_neighbors()
+    o.search_neighbors()
+    gi, gj = g.pairs()
+    oi, oj = o.pairs()
+    assert len(gi) > n
+    assert np.array_equal(gi, oi) and np.array_equal(gj, oj)
+    sg = g.get_state()
+    int_rows_equal(sg, o.get_state())
+    assert set(zip(gi.tolist(), gj.tolist())) == brute_pairs(cfg, sg)
+
+
 def test_search_dense_cluster_in_sparse_grid(oracle_mod):
     """A 3D grid that is sparse on average (six cells per axis) with one
     crowded spot: a large bubble in a shell of 300 small ones. The home cell
