@@ -26,6 +26,14 @@
 //   --array FILE             expand an array.params file
 //                            (scripts/triton/array_job.py:54-75) into one
 //                            run per parameter set, each in run_<k>/.
+//   --profile-range          the reference's PROFILE build option as a flag:
+//                            the profiler's capture range (cudaProfilerStart /
+//                            Stop) opens when the step loop starts and closes
+//                            after 1000 steps within one time unit or after
+//                            the loop's first printed time unit
+//                            (src/util.cuh:38-52, src/simulator.cu:993,
+//                            :1009)
+#include <cuda_profiler_api.h>
 #include <cuda_runtime.h>
 #include <curand.h>
 #include <nvtx3/nvToolsExt.h>
@@ -55,6 +63,8 @@ constexpr double kPi = 3.1415926535897932384626433832795028841971693993;
 
 // Significant digits of the output files (--output-digits).
 int g_output_digits = 6;
+// --profile-range: open the profiler's capture range over the step loop.
+bool g_profile_range = false;
 
 void check(int rc, const char *what) {
     if (rc != CB_OK)
@@ -601,6 +611,11 @@ void simulate(Run &r) {
     int64_t steps_in_time_step = 0, total = 0;
     cb_report rep = report(r);
     int64_t searches0 = rep.searches;
+    // CUBBLE_PROFILE: start here; stop after 1000 steps in a time unit or
+    // once the loop has printed (the reference's timesPrinted == 2)
+    bool profiling = false;
+    if (g_profile_range) profiling = cudaProfilerStart() == cudaSuccess;
+    constexpr int64_t kProfileSteps = 1000;
     while (cont) {
         // the next output time: a printed time unit or a snapshot
         uint64_t pi = 0, si = 0;
@@ -620,7 +635,8 @@ void simulate(Run &r) {
         }
         stop.min_count = r.min_num_bubbles;
         stop.max_radius = min_interval;
-        const int64_t limit = r.max_steps > 0 ? r.max_steps - total : INT64_MAX / 2;
+        int64_t limit = r.max_steps > 0 ? r.max_steps - total : INT64_MAX / 2;
+        if (profiling) limit = std::min(limit, kProfileSteps - steps_in_time_step);
         const int64_t steps0 = rep.steps;
         check(cb_integrate_until(r.ctx, limit, &stop, &rep), "cb_integrate_until");
         const int64_t k = rep.steps - steps0;
@@ -675,8 +691,13 @@ void simulate(Run &r) {
             check(cb_reset_rows(r.ctx, CB_RESET_ERROR), "cb_reset_rows");
             if (!r.checkpoint.empty()) write_checkpoint(r, r.checkpoint);
         }
+        if (profiling && (steps_in_time_step >= kProfileSteps || r.times_printed >= 2)) {
+            cudaProfilerStop();
+            profiling = false;
+        }
         if (r.max_steps > 0 && total >= r.max_steps) break;
     }
+    if (profiling) cudaProfilerStop();
     if (rep.count <= r.min_num_bubbles) {
         std::printf("Stopping simulation, since the number of bubbles left in the simulation (%d) "
                     "is less than or equal to the specified minimum (%d)\n",
@@ -795,6 +816,8 @@ int main(int argc, char **argv) {
                     throw std::runtime_error("--output-digits must be 1 ... 17");
             } else if (s == "--array") {
                 array = next();
+            } else if (s == "--profile-range") {
+                g_profile_range = true;
             } else if (input.empty()) {
                 input = s;
             } else {

@@ -150,6 +150,25 @@ def test_cli_checkpoint_resume_continues(tmp_path):
     del steps_to_ck
 
 
+def test_cli_profile_range_keeps_results(tmp_path):
+    """--profile-range (the reference's PROFILE option: the profiler's capture
+    range over the first stretch of the step loop) ends the graph stretches
+    at its stop step and changes nothing else: results.dat matches the run
+    without it to the rounding of the FP64 reductions (whose order is free
+    from run to run)."""
+    a = os.path.join(str(tmp_path), "a")
+    b = os.path.join(str(tmp_path), "b")
+    os.makedirs(a)
+    os.makedirs(b)
+    inp = small_input()
+    run_cli(a, ["input.json", "--max-steps", "2500", "--output-digits", "17"], inp)
+    run_cli(b, ["input.json", "--max-steps", "2500", "--output-digits", "17", "--profile-range"],
+            inp)
+    ra, rb = results(a), results(b)
+    assert ra.shape == rb.shape and len(ra) >= 2
+    np.testing.assert_allclose(rb, ra, rtol=1e-9, atol=1e-12)
+
+
 def test_cli_array_jobs(tmp_path):
     tmp = str(tmp_path)
     with open(os.path.join(tmp, "array.params"), "w") as f:
