@@ -685,7 +685,7 @@ CB_KERNEL_PAIR((template <int DIM>), k_pair_rows, (<DIM>), __launch_bounds__(kBl
 // cell's stencil offset times the cell edge, across a periodic face too
 // (four or more cells per axis make the offset unique): the FP32 rounding
 // is relative to a cell edge, not to the box, and the guard band where the
-// reference's FP64 test decides is ~50x narrower. The home cell's bubbles are
+// reference's FP64 test decides is ~40x narrower. The home cell's bubbles are
 // then broadcast from shared memory one at a time and every lane tests its
 // candidate against the bubble; the warp's hit mask of each (bubble, chunk)
 // goes to shared memory, and after a window of up to kTileChunks chunks each
