@@ -83,6 +83,7 @@ struct DevConst {
     float kq_f;  // K / (4 pi) in 3D, K / (2 pi) in 2D, as FP32
     float pre_margin;  // FP32 pair-search prefilter margin (length units)
     long long lbq[3];  // the box's lower corner in fixed point (x 2^40)
+    int fix_range;     // box corners within 2^21: coordinates fit the fixed point
     float half_iv32[3];
     float iv32[3];
     // Linear shear flow (cb_config.shear_speed): v_x += shear (2 (q - lbb_q)

@@ -100,6 +100,9 @@ void fill_const(cb_context *c) {
     // The squared-distance and cutoff roundings add < 1e-6 absolute.
     // 2e-6 (maxabs + L) + 1e-5 is about 4x the worst case.
     k.pre_margin = (float)(2e-6 * (maxabs + maxiv) + 1e-5);
+    // fix_from_double needs |x| < 2^23: box corners within 2^21 leave room
+    // for bubbles past a wall
+    k.fix_range = maxabs < 2097152.0 ? 1 : 0;
     k.shear_on = f.shear_speed != 0.0 ? 1 : 0;
     k.shear_axis = k.dim - 1;
     k.shear = f.shear_speed;

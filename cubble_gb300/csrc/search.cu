@@ -243,11 +243,13 @@ __device__ __forceinline__ void gather_rate(const Bufs &b, const Ctrl *c, int fr
 }
 
 // Sparse 3D grids whose periodic axes have at least four cells (and fewer
-// than 2^26 cells) are counted by k_pair_tiles: a neighbour cell is then
-// reached through at most one periodic image, and never twice.
+// than 2^26 cells, in a box whose corners lie within 2^21 of the origin) are
+// counted by k_pair_tiles: a neighbour cell is then reached through at most
+// one periodic image, and never twice.
 template <int DIM>
 __device__ __forceinline__ bool tile_grid(const DevConst &k, const int cd[3], int ncell) {
-    bool ok = DIM == 3 && ncell < (1 << 26);  // cell index and stencil offset in one sort key
+    // cell index and stencil offset in one sort key; fixed-point coordinates
+    bool ok = DIM == 3 && ncell < (1 << 26) && k.fix_range;
 #pragma unroll
     for (int a = 0; a < DIM; a++) ok &= k.wall[a] || cd[a] >= 4;
     return ok;
