@@ -42,6 +42,7 @@ enum DRole : int {
     RVP0, RVP1, RVP2, RVP3,      // dxdtp ... (this attempt)
     RPATH, RPATHN, RERR, RERR2,  // path, pathNew, error, spare
     RS0, RS1, RS2, RS3,          // saved position / radius of the last search
+    RVQ0, RVQ1, RVQ2, RVQ3,      // spares: the search's gather of the previous rates
     ND_ROLES
 };
 enum IRole : int {

@@ -16,7 +16,7 @@ const char *status_text(int s);
 // Kernels per phase (for the launch counter of graph executions).
 constexpr int kKernelsPerAttempt = 3;
 constexpr int kKernelsPerRemove = 9;
-constexpr int kKernelsPerSearch = 17;
+constexpr int kKernelsPerSearch = 16;
 // Count of C-ABI calls that may touch a context, process wide: a context
 // whose host mirror was left current by a call knows, by this count, that no
 // call has run since.

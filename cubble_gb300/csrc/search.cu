@@ -228,20 +228,6 @@ __device__ __forceinline__ void k_cell_order_body(const Bufs &b, const int vb, c
 CB_KERNEL_PAIR((), k_cell_order, (), __launch_bounds__(kBlock))
 
 
-// Gathers a rate row (FP64, or FP32 in the mixed form) into another slot.
-__device__ __forceinline__ void gather_rate(const Bufs &b, const Ctrl *c, int from_role,
-                                            int to_role, const int *src, int n, int vb, int vg) {
-    const bool f32 = b.k->mixed;
-    const double *from = drow(b, c, from_role);
-    double *to = drow(b, c, to_role);
-    for (int q = vb * blockDim.x + threadIdx.x; q < n; q += vg * blockDim.x) {
-        if (f32)
-            reinterpret_cast<float *>(to)[q] = reinterpret_cast<const float *>(from)[src[q]];
-        else
-            to[q] = from[src[q]];
-    }
-}
-
 // Sparse 3D grids whose periodic axes have at least four cells (and fewer
 // than 2^26 cells, in a box whose corners lie within 2^21 of the origin) are
 // counted by k_pair_tiles: a neighbour cell is then reached through at most
@@ -255,12 +241,13 @@ __device__ __forceinline__ bool tile_grid(const DevConst &k, const int cd[3], in
     return ok;
 }
 
-// Gather pass A: positions (+ saved), velocities, path, error, wrap counts
-// and indices into their spare slots, then swap the roles. One pass over
-// the bubbles: every row of a bubble is gathered in the same iteration (the
-// permutation read once, all loads of the bubble in flight together).
+// Gather of every persistent row into cell order: positions (+ saved),
+// velocities, previous velocities, path, error, wrap counts and indices into
+// their spare slots, then swap the roles. One pass over the bubbles: every
+// row of a bubble is gathered in the same iteration (the permutation read
+// once, all loads of the bubble in flight together).
 template <int DIM>
-__device__ __forceinline__ void k_permute_a_body(const Bufs &b, const int vb, const int vg) {
+__device__ __forceinline__ void k_permute_body(const Bufs &b, const int vb, const int vg) {
     Ctrl *c = b.ctrl;
     const int n = c->n;
     const int *src = b.permSorted;
@@ -268,8 +255,8 @@ __device__ __forceinline__ void k_permute_a_body(const Bufs &b, const int vb, co
     const int roles[4][2] = {{RX, RXN}, {RY, RYN}, {RZ, RZN}, {RR, RRN}};
     const double *pf[4];
     double *pt[4], *sv[4];
-    const double *vf[4];
-    double *vt[4];
+    const double *vf[4], *of[4];
+    double *vt[4], *ot[4];
 #pragma unroll
     for (int a = 0; a < 4; a++) {
         pf[a] = drow(b, c, roles[a][0]);
@@ -277,6 +264,8 @@ __device__ __forceinline__ void k_permute_a_body(const Bufs &b, const int vb, co
         sv[a] = drow(b, c, RS0 + a);
         vf[a] = drow(b, c, RV0 + a);
         vt[a] = drow(b, c, RVP0 + a);
+        of[a] = drow(b, c, RVO0 + a);
+        ot[a] = drow(b, c, RVQ0 + a);
     }
     const double *f1 = drow(b, c, RPATH), *f2 = drow(b, c, RERR);
     double *t1 = drow(b, c, RPATHN), *t2 = drow(b, c, RERR2);
@@ -284,7 +273,8 @@ __device__ __forceinline__ void k_permute_a_body(const Bufs &b, const int vb, co
     int *ti[4] = {irow(b, c, IWX2), irow(b, c, IWY2), irow(b, c, IWZ2), irow(b, c, IIDX2)};
     // for the 3D tile pass: x, y, z relative to the lower corner of the
     // bubble's cell, from exact fixed-point differences (x 2^40; the cell
-    // edge L / cd in that unit, off by at most one unit)
+    // edge L / cd in that unit, off by at most one unit); the FP32 copy of
+    // the positions is for the other passes
     const DevConst &k = *b.k;
     const int cd[3] = {c->cell_dims[0], c->cell_dims[1], c->cell_dims[2]};
     const bool rel = DIM == 3 && c->sparse_cells && tile_grid<DIM>(k, cd, c->ncell);
@@ -299,15 +289,18 @@ __device__ __forceinline__ void k_permute_a_body(const Bufs &b, const int vb, co
         double p[4];
 #pragma unroll
         for (int a = 0; a < 4; a++) p[a] = (DIM == 2 && a == 2) ? 0.0 : pf[a][s];
-        double v[4];
-        float vf32[4];
+        double v[4], vo[4];
+        float vf32[4], vo32[4];
 #pragma unroll
         for (int a = 0; a < 4; a++) {
             if (DIM == 2 && a == 2) continue;
-            if (f32)
+            if (f32) {
                 vf32[a] = reinterpret_cast<const float *>(vf[a])[s];
-            else
+                vo32[a] = reinterpret_cast<const float *>(of[a])[s];
+            } else {
                 v[a] = vf[a][s];
+                vo[a] = of[a][s];
+            }
         }
         const double g1 = f1[s], g2 = f2[s];
         const int w0 = fi[0][s], w1 = fi[1][s], w2 = fi[2][s], w3 = fi[3][s];
@@ -316,10 +309,13 @@ __device__ __forceinline__ void k_permute_a_body(const Bufs &b, const int vb, co
             if (DIM == 2 && a == 2) continue;
             pt[a][q] = p[a];
             sv[a][q] = p[a];
-            if (f32)
+            if (f32) {
                 reinterpret_cast<float *>(vt[a])[q] = vf32[a];
-            else
+                reinterpret_cast<float *>(ot[a])[q] = vo32[a];
+            } else {
                 vt[a][q] = v[a];
+                ot[a][q] = vo[a];
+            }
         }
         t1[q] = g1;
         t2[q] = g2;
@@ -327,9 +323,10 @@ __device__ __forceinline__ void k_permute_a_body(const Bufs &b, const int vb, co
         ti[1][q] = w1;
         ti[2][q] = w2;
         ti[3][q] = w3;
-        b.pos32[q] = make_float4((float)p[0], (float)p[1], DIM == 3 ? (float)p[2] : 0.0f,
-                                 (float)p[3]);
-        if (rel) {
+        if (!rel) {
+            b.pos32[q] = make_float4((float)p[0], (float)p[1], DIM == 3 ? (float)p[2] : 0.0f,
+                                     (float)p[3]);
+        } else {
             const int cell = b.cellSorted[q];
             const int kc[3] = {cell % cd[0], (cell / cd[0]) % cd[1], cell / (cd[0] * cd[1])};
             float o[3];
@@ -345,6 +342,7 @@ __device__ __forceinline__ void k_permute_a_body(const Bufs &b, const int vb, co
             if (DIM == 2 && a == 2) continue;
             swap_role(r, roles[a][0], roles[a][1]);
             swap_role(r, RV0 + a, RVP0 + a);
+            swap_role(r, RVO0 + a, RVQ0 + a);
         }
         swap_role(r, RPATH, RPATHN);
         swap_role(r, RERR, RERR2);
@@ -356,28 +354,9 @@ __device__ __forceinline__ void k_permute_a_body(const Bufs &b, const int vb, co
         c->done[DC_PERMUTE] = 0;
     }
 }
-CB_KERNEL_PAIR((template <int DIM>), k_permute_a, (<DIM>), __launch_bounds__(kBlock, 4))
+CB_KERNEL_PAIR((template <int DIM>), k_permute, (<DIM>), __launch_bounds__(kBlock, 3))
 
 
-// Gather pass B: previous velocities into the slot the old velocities left.
-template <int DIM>
-__device__ __forceinline__ void k_permute_b_body(const Bufs &b, const int vb, const int vg) {
-    Ctrl *c = b.ctrl;
-    const int n = c->n;
-    const int *src = b.permSorted;
-    for (int a = 0; a < 4; a++) {
-        if (DIM == 2 && a == 2) continue;
-        gather_rate(b, c, RVO0 + a, RVP0 + a, src, n, vb, vg);
-    }
-    if (last_block(&c->done[DC_PERMUTE], vg) && threadIdx.x == 0) {
-        for (int a = 0; a < 4; a++) {
-            if (DIM == 2 && a == 2) continue;
-            swap_role(c->drole, RVO0 + a, RVP0 + a);
-        }
-        c->done[DC_PERMUTE] = 0;
-    }
-}
-CB_KERNEL_PAIR((template <int DIM>), k_permute_b, (<DIM>), __launch_bounds__(kBlock))
 
 
 // Neighbour cell `k` (0..26, offsets dx,dy,dz in -1..1) of `cell`, or
@@ -497,6 +476,13 @@ __device__ __forceinline__ void k_pair_cells_body(const Bufs &b, const int vb, c
     const int pcap = k.pcap;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int warps = vg * kWarpsPerBlock;
+    // The FP32 positions: the gather's copy, or, where the tile pass counted
+    // (its gather wrote only cell-relative coordinates), the same values
+    // converted here from the FP64 rows
+    const bool conv = WRITE && DIM == 3 && c->sparse_cells && tile_grid<DIM>(k, cd, ncell);
+    auto pos_f = [&](int q) {
+        return conv ? make_float4((float)X[q], (float)Y[q], (float)Z[q], (float)R[q]) : b.pos32[q];
+    };
     for (int cell = vb * kWarpsPerBlock + w; cell < ncell; cell += warps) {
         const int s0 = b.cellStart[cell], e0 = b.cellStart[cell + 1];
         if (s0 == e0) continue;
@@ -508,7 +494,7 @@ __device__ __forceinline__ void k_pair_cells_body(const Bufs &b, const int vb, c
             float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
             int base = 0, cnt = 0;
             if (active) {
-                pi = b.pos32[i];
+                pi = pos_f(i);
                 if (WRITE) base = b.rowStart[i];
             }
             for (int qn = 0; qn < m; qn++) {
@@ -517,7 +503,7 @@ __device__ __forceinline__ void k_pair_cells_body(const Bufs &b, const int vb, c
                 for (int c0 = cs; c0 < ce; c0 += 32) {
                     const int nc = min(32, ce - c0);
                     __syncwarp();
-                    if (lane < nc) stage[w][lane] = b.pos32[c0 + lane];
+                    if (lane < nc) stage[w][lane] = pos_f(c0 + lane);
                     __syncwarp();
                     for (int t = 0; t < nc; t++) {
                         const int j = c0 + t;
@@ -748,11 +734,34 @@ __device__ __forceinline__ void tile_exact(const DevConst &k, const float4 *home
     __syncwarp();
 }
 
+// Each lane (home bubble lane < nh) appends its partners among the tc
+// tested chunks of a window to its row, in candidate order.
+template <int M>
+__device__ __forceinline__ void tile_rows(const unsigned (*hitmask)[32], const int *candj, int tc,
+                                          int nh, int *row, int &mycnt) {
+    const int lane = threadIdx.x & 31;
+    __syncwarp();
+    if (lane < nh) {
+        for (int ch = 0; ch < tc; ch++) {
+            unsigned hm = hitmask[ch][lane];
+            while (hm) {
+                const int bit = __ffs(hm) - 1;
+                hm &= hm - 1;
+                if (mycnt < M) row[mycnt] = candj[(ch << 5) + bit];
+                mycnt++;
+            }
+        }
+    }
+    __syncwarp();
+}
+
 template <int DIM>
 __device__ __forceinline__ void k_pair_tiles_body(const Bufs &b, const int vb, const int vg) {
     __shared__ float4 home[kWarpsPerBlock][32];
     __shared__ unsigned hitmask[kWarpsPerBlock][kTileChunks][32];  // [chunk][home bubble]
     __shared__ int candj[kWarpsPerBlock][kTileChunks * 32];
+    __shared__ float4 stp[kWarpsPerBlock][64];  // kept candidates (home frame)
+    __shared__ int stj[kWarpsPerBlock][64];
     Ctrl *c = b.ctrl;
     if (!c->sparse_cells) return;
     const DevConst &k = *b.k;
@@ -840,63 +849,106 @@ __device__ __forceinline__ void k_pair_tiles_body(const Bufs &b, const int vb, c
             if (lane >= o) pre += t;
         }
         const int T = __shfl_sync(kAll, pre, 31);  // lanes >= m add nothing
-        const int nhome = e0 - s0;                  // the home cell is the first
         for (int h0 = s0; h0 < e0; h0 += 32) {
             const int nh = min(32, e0 - h0);
             __syncwarp();
-            if (lane < nh) home[w][lane] = pos[h0 + lane];
+            float4 ph = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (lane < nh) {
+                ph = pos[h0 + lane];
+                home[w][lane] = ph;
+            }
+            // the box around the home bubbles and their largest radius: a
+            // candidate farther from the box than that radius + its own +
+            // skin + pad pairs with none of them, and is dropped before the
+            // tests (pad = 4 band covers the FP32 error of the tests, so the
+            // exact test would refuse every dropped pair)
+            const bool hv = lane < nh;
+            float blo[3] = {hv ? ph.x : 3.4e38f, hv ? ph.y : 3.4e38f, hv ? ph.z : 3.4e38f};
+            float bhi[3] = {hv ? ph.x : -3.4e38f, hv ? ph.y : -3.4e38f, hv ? ph.z : -3.4e38f};
+            float rh = hv ? ph.w : 0.f;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    blo[a] = fminf(blo[a], __shfl_xor_sync(kAll, blo[a], o));
+                    bhi[a] = fmaxf(bhi[a], __shfl_xor_sync(kAll, bhi[a], o));
+                }
+                rh = fmaxf(rh, __shfl_xor_sync(kAll, rh, o));
+            }
+            const float reach0 = rh + skin + 4.f * band;
             __syncwarp();
             int mycnt = 0;  // partners of home bubble h0 + lane so far
-            for (int w0 = 0; w0 < T; w0 += kTileChunks * 32) {
-                const int nch = min(kTileChunks, (T - w0 + 31) >> 5);
-                for (int ch = 0; ch < nch; ch++) {
-                    const int bb = w0 + (ch << 5) + lane;
-                    // the cell of candidate bb: the number of cells whose
-                    // inclusive prefix is <= bb (pre ascends over the lanes)
-                    int t = 0;
+            int *row = stash + (size_t)(h0 + min(lane, nh - 1)) * M;
+            // kept candidates wait in a ring of 64 (in candidate order) until
+            // 32 of them fill a chunk; tc chunks are tested in the window
+            int ns = 0, head = 0, tc = 0;
+            for (int r0 = 0; r0 < T; r0 += 32) {
+                const int bb = r0 + lane;
+                // the cell of candidate bb: the number of cells whose
+                // inclusive prefix is <= bb (pre ascends over the lanes)
+                int t = 0;
 #pragma unroll
-                    for (int step = 16; step > 0; step >>= 1)
-                        if (__shfl_sync(kAll, pre, t + step - 1) <= bb) t += step;
-                    const int ct = __shfl_sync(kAll, cs, t), pt = __shfl_sync(kAll, pre, t),
-                              nt = __shfl_sync(kAll, cn, t), kt = __shfl_sync(kAll, key, t);
-                    int j = -1;
-                    // an unused lane tests a point far outside the box
-                    float4 pj = make_float4(1e18f, 1e18f, 1e18f, 0.f);
-                    if (bb < T) {
-                        j = ct + bb - (pt - nt);
-                        pj = pos[j];
-                        const int o = kt & 31;
-                        pj.x = fmaf((float)(o % 3 - 1), cw[0], pj.x);
-                        pj.y = fmaf((float)((o / 3) % 3 - 1), cw[1], pj.y);
-                        pj.z = fmaf((float)(o / 9 - 1), cw[2], pj.z);
-                    }
-                    candj[w][(ch << 5) + lane] = j;
-                    const float wj = pj.w + skin;
-                    const bool amb = w0 + (ch << 5) < nhome  // home cell bubbles: only j > i
-                                         ? tile_tests<true>(home[w], nh, h0, j, pj, wj, tb,
-                                                            hitmask[w][ch])
-                                         : tile_tests<false>(home[w], nh, h0, j, pj, wj, tb,
-                                                             hitmask[w][ch]);
-                    if (amb)
-                        tile_exact<DIM>(k, home[w], nh, h0, j, pj, wj, tb, hitmask[w][ch], X,
-                                        Y, Z, R);
+                for (int step = 16; step > 0; step >>= 1)
+                    if (__shfl_sync(kAll, pre, t + step - 1) <= bb) t += step;
+                const int ct = __shfl_sync(kAll, cs, t), pt = __shfl_sync(kAll, pre, t),
+                          nt = __shfl_sync(kAll, cn, t), kt = __shfl_sync(kAll, key, t);
+                int j = -1;
+                float4 pj = make_float4(0.f, 0.f, 0.f, 0.f);
+                bool keep = false;
+                if (bb < T) {
+                    j = ct + bb - (pt - nt);
+                    pj = pos[j];
+                    const int o = kt & 31;
+                    pj.x = fmaf((float)(o % 3 - 1), cw[0], pj.x);
+                    pj.y = fmaf((float)((o / 3) % 3 - 1), cw[1], pj.y);
+                    pj.z = fmaf((float)(o / 9 - 1), cw[2], pj.z);
+                    const float ex = fmaxf(fmaxf(blo[0] - pj.x, pj.x - bhi[0]), 0.f);
+                    const float ey = fmaxf(fmaxf(blo[1] - pj.y, pj.y - bhi[1]), 0.f);
+                    const float ez = fmaxf(fmaxf(blo[2] - pj.z, pj.z - bhi[2]), 0.f);
+                    const float reach = reach0 + pj.w;
+                    keep = fmaf(ez, ez, fmaf(ey, ey, ex * ex)) <= reach * reach;
                 }
-                __syncwarp();
-                // each lane appends its home bubble's partners of the window
-                if (lane < nh) {
-                    int *row = stash + (size_t)(h0 + lane) * M;
-                    for (int ch = 0; ch < nch; ch++) {
-                        unsigned hm = hitmask[w][ch][lane];
-                        while (hm) {
-                            const int bit = __ffs(hm) - 1;
-                            hm &= hm - 1;
-                            if (mycnt < M) row[mycnt] = candj[w][(ch << 5) + bit];
-                            mycnt++;
-                        }
+                const unsigned km = __ballot_sync(kAll, keep);
+                if (keep) {
+                    const int s = (head + ns + __popc(km & ((1u << lane) - 1u))) & 63;
+                    stj[w][s] = j;
+                    stp[w][s] = pj;
+                }
+                ns += __popc(km);
+                const bool last = r0 + 32 >= T;
+                while (ns >= 32 || (last && ns > 0)) {
+                    __syncwarp();
+                    const int s = (head + lane) & 63;
+                    int jt = -1;
+                    // an unused lane tests a point far outside the box
+                    float4 pt4 = make_float4(1e18f, 1e18f, 1e18f, 0.f);
+                    if (lane < ns) {
+                        jt = stj[w][s];
+                        pt4 = stp[w][s];
+                    }
+                    candj[w][(tc << 5) + lane] = jt;
+                    const float wj = pt4.w + skin;
+                    // home cell bubbles (only j > i) come first, and only they
+                    // lie below e0
+                    const bool amb = __shfl_sync(kAll, jt, 0) < e0
+                                         ? tile_tests<true>(home[w], nh, h0, jt, pt4, wj, tb,
+                                                            hitmask[w][tc])
+                                         : tile_tests<false>(home[w], nh, h0, jt, pt4, wj, tb,
+                                                             hitmask[w][tc]);
+                    if (amb)
+                        tile_exact<DIM>(k, home[w], nh, h0, jt, pt4, wj, tb, hitmask[w][tc], X,
+                                        Y, Z, R);
+                    head = (head + 32) & 63;
+                    ns = max(ns - 32, 0);
+                    if (++tc == kTileChunks) {
+                        tile_rows<M>(hitmask[w], candj[w], tc, nh, row, mycnt);
+                        tc = 0;
                     }
                 }
                 __syncwarp();
             }
+            if (tc > 0)
+                tile_rows<M>(hitmask[w], candj[w], tc, nh, row, mycnt);
             if (lane < nh) {
                 const int i = h0 + lane;
                 NN[i] = mycnt;
@@ -999,14 +1051,12 @@ void launch_search(const Launch &l, const Bufs &b, int dim) {
     CB_LAUNCH(l, k_cell_fill, (), G, b);
     CB_LAUNCH(l, k_cell_order, (), G, b);
     if (dim == 3) {
-        CB_LAUNCH(l, k_permute_a, (<3>), G, b);
-        CB_LAUNCH(l, k_permute_b, (<3>), G, b);
+        CB_LAUNCH(l, k_permute, (<3>), G, b);
         CB_LAUNCH(l, k_pair_cells, (<3, false>), G, b);
         CB_LAUNCH(l, k_pair_tiles, (<3>), G, b);
         CB_LAUNCH(l, k_pair_rows, (<3>), G, b);
     } else {
-        CB_LAUNCH(l, k_permute_a, (<2>), G, b);
-        CB_LAUNCH(l, k_permute_b, (<2>), G, b);
+        CB_LAUNCH(l, k_permute, (<2>), G, b);
         CB_LAUNCH(l, k_pair_cells, (<2, false>), G, b);
         CB_LAUNCH(l, k_pair_rows, (<2>), G, b);
     }
