@@ -6,15 +6,18 @@
 //   k_cell_fill   counting-sort scatter (indexByCell, src/kernels.cu:609-615)
 //   k_cell_order  one warp per cell orders its bubbles by previous position,
 //                 so the cell order is deterministic
-//   k_permute_*   gather every persistent row into cell order and set
-//                 saved := positions (reorganizeByIndex, src/kernels.cu:721-770);
-//                 the pointer rotation of src/simulator.cu:99-146 becomes a
-//                 role swap in the control block
-//   k_pair_cells  per bubble, the pairs (i, j > i) within r_i + r_j + skin
-//                 (neighborSearch / comparePair, src/kernels.cu:617-701):
-//                 one enumeration that counts each row and keeps its
-//                 partners, a scan, k_pair_compact writing the rows, so the
-//                 list is ordered by (i, j) without atomics (a second
+//   k_permute     gather every persistent row into cell order in one pass and
+//                 set saved := positions (reorganizeByIndex,
+//                 src/kernels.cu:721-770); the pointer rotation of
+//                 src/simulator.cu:99-146 becomes a role swap in the control
+//                 block
+//   k_pair_cells, k_pair_tiles, k_pair_rows
+//                 per bubble, the pairs (i, j > i) within r_i + r_j + skin
+//                 (neighborSearch / comparePair, src/kernels.cu:617-701),
+//                 by the pass that suits the grid (dense cells, sparse 3D,
+//                 sparse 2D): one enumeration that counts each row and keeps
+//                 its partners, a scan, k_pair_compact writing the rows, so
+//                 the list is ordered by (i, j) without atomics (a second
 //                 enumeration only when a row outgrew its stash); candidates
 //                 are screened in FP32 with a conservative margin and
 //                 accepted by the exact FP64 test of the reference, so the
