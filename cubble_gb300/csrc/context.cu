@@ -557,10 +557,10 @@ int cb_load_state(cb_context *c, const cb_state_view *s) {
     drows[RVO3] = s->drdto;
     drows[RPATH] = s->path;
     drows[RERR] = s->error;
-    drows[RS0] = s->saved_x ? s->saved_x : s->x;
-    drows[RS1] = s->saved_y ? s->saved_y : s->y;
-    drows[RS2] = s->saved_z ? s->saved_z : s->z;
-    drows[RS3] = s->saved_r ? s->saved_r : s->r;
+    drows[RS0] = s->saved_x;
+    drows[RS1] = s->saved_y;
+    drows[RS2] = s->saved_z;
+    drows[RS3] = s->saved_r;
     std::vector<std::vector<float>> fl;
     for (int r = 0; r < ND_ROLES; r++) {
         double *dst = c->dslot[h.drole[r]];
@@ -571,6 +571,11 @@ int cb_load_state(cb_context *c, const cb_state_view *s) {
                                     c->stream));
         } else if (drows[r]) {
             CB_CUDA(cudaMemcpyAsync(dst, drows[r], n * 8, cudaMemcpyHostToDevice, c->stream));
+        } else if (r >= RS0 && r <= RS3 && n && drows[RX + (r - RS0)]) {
+            // saved position / radius not given: the uploaded current ones,
+            // copied on the device
+            CB_CUDA(cudaMemcpyAsync(dst, c->dslot[h.drole[RX + (r - RS0)]], n * 8,
+                                    cudaMemcpyDeviceToDevice, c->stream));
         } else {
             CB_CUDA(cudaMemsetAsync(dst, 0, (size_t)c->hk.cap * 8, c->stream));
         }
