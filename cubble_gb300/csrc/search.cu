@@ -852,6 +852,16 @@ __device__ __forceinline__ void k_pair_tiles_body(const Bufs &b, const int vb, c
             if (lane >= o) pre += t;
         }
         const int T = __shfl_sync(kAll, pre, 31);  // lanes >= m add nothing
+        // lane t: candidate bb of its cell is bubble cbase + bb; the cell's
+        // move into the home frame
+        const int cbase = cs - (pre - cn);
+        float mvx = 0.f, mvy = 0.f, mvz = 0.f;
+        {
+            const int o = key & 31;
+            mvx = (float)(o % 3 - 1) * cw[0];
+            mvy = (float)((o / 3) % 3 - 1) * cw[1];
+            mvz = (float)(o / 9 - 1) * cw[2];
+        }
         for (int h0 = s0; h0 < e0; h0 += 32) {
             const int nh = min(32, e0 - h0);
             __syncwarp();
@@ -893,18 +903,18 @@ __device__ __forceinline__ void k_pair_tiles_body(const Bufs &b, const int vb, c
 #pragma unroll
                 for (int step = 16; step > 0; step >>= 1)
                     if (__shfl_sync(kAll, pre, t + step - 1) <= bb) t += step;
-                const int ct = __shfl_sync(kAll, cs, t), pt = __shfl_sync(kAll, pre, t),
-                          nt = __shfl_sync(kAll, cn, t), kt = __shfl_sync(kAll, key, t);
+                const int bt = __shfl_sync(kAll, cbase, t);
+                const float mx = __shfl_sync(kAll, mvx, t), my = __shfl_sync(kAll, mvy, t),
+                            mz = __shfl_sync(kAll, mvz, t);
                 int j = -1;
                 float4 pj = make_float4(0.f, 0.f, 0.f, 0.f);
                 bool keep = false;
                 if (bb < T) {
-                    j = ct + bb - (pt - nt);
+                    j = bt + bb;
                     pj = pos[j];
-                    const int o = kt & 31;
-                    pj.x = fmaf((float)(o % 3 - 1), cw[0], pj.x);
-                    pj.y = fmaf((float)((o / 3) % 3 - 1), cw[1], pj.y);
-                    pj.z = fmaf((float)(o / 9 - 1), cw[2], pj.z);
+                    pj.x += mx;
+                    pj.y += my;
+                    pj.z += mz;
                     const float ex = fmaxf(fmaxf(blo[0] - pj.x, pj.x - bhi[0]), 0.f);
                     const float ey = fmaxf(fmaxf(blo[1] - pj.y, pj.y - bhi[1]), 0.f);
                     const float ez = fmaxf(fmaxf(blo[2] - pj.z, pj.z - bhi[2]), 0.f);
