@@ -145,6 +145,7 @@ struct cb_batch {
     int *dlists = nullptr;
     cudaGraphExec_t gexec = nullptr;
     int graph_tile = -1;
+    cbg::PhaseKernels graph_kernels;
     int tile = 2048;
     int gmax = 1;  // blocks of every batched launch
     long long launches = 0;
@@ -226,7 +227,8 @@ int build_batch_graph(cb_batch *b) {
     cudaStream_t s = b->stream;
     CB_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0,
                                           cudaStreamCaptureModeThreadLocal));
-    launch_batch_attempt(b, &dummy);
+    launch_batch_attempt(b, &dummy);  // the attempt kernels and the decision
+    const long long n_attempt = dummy;
     cudaGraph_t delbody, searchbody, out;
     int rc = capture_conditional(s, cudaGraphCondTypeIf, &hdel, 0, &delbody);
     if (!rc) rc = capture_conditional(s, cudaGraphCondTypeIf, &hsearch, 0, &searchbody);
@@ -236,10 +238,14 @@ int build_batch_graph(cb_batch *b) {
     CB_CUDA(cudaStreamBeginCaptureToGraph(s, delbody, nullptr, nullptr, 0,
                                           cudaStreamCaptureModeThreadLocal));
     launch_batch_remove(b, &dummy);
+    const long long n_remove = dummy - n_attempt;
     CB_CUDA(cudaStreamEndCapture(s, &out));
     CB_CUDA(cudaStreamBeginCaptureToGraph(s, searchbody, nullptr, nullptr, 0,
                                           cudaStreamCaptureModeThreadLocal));
     launch_batch_search(b, &dummy);
+    b->graph_kernels.attempt = n_attempt;
+    b->graph_kernels.remove = n_remove;
+    b->graph_kernels.search = dummy - n_attempt - n_remove;
     CB_CUDA(cudaStreamEndCapture(s, &out));
     CB_CUDA(cudaGraphInstantiate(&b->gexec, g, 0));
     CB_CUDA(cudaGraphUpload(b->gexec, b->stream));
@@ -330,9 +336,9 @@ int batch_integrate(cb_batch *b, int64_t n_steps, cb_report *reports, double *ms
     if (graph && n_steps > 0) {
         // attempt kernels + decide per loop iteration; a remove / search
         // phase is one launch of each of its kernels for all foams together
-        b->launches += b->hbc->decides * (kKernelsPerAttempt + 1);
-        b->launches += b->hbc->any_delete_phases * kKernelsPerRemove;
-        b->launches += b->hbc->any_search_phases * kKernelsPerSearch;
+        b->launches += b->hbc->decides * b->graph_kernels.attempt;
+        b->launches += b->hbc->any_delete_phases * b->graph_kernels.remove;
+        b->launches += b->hbc->any_search_phases * b->graph_kernels.search;
     }
     return batch_fail_status(b);
 }

@@ -275,6 +275,7 @@ int build_graph(cb_context *c) {
                                           cudaStreamCaptureModeThreadLocal));
     const int dim = c->hk.dim;
     launch_attempt_kernels(c, l, c->bufs);
+    const long long n_attempt = dummy;
     cudaGraph_t delbody, searchbody;
     int rc = capture_conditional(s, cudaGraphCondTypeIf, &hdel, 0, &delbody);
     if (!rc) rc = capture_conditional(s, cudaGraphCondTypeIf, &hsearch, 0, &searchbody);
@@ -285,10 +286,14 @@ int build_graph(cb_context *c) {
     CB_CUDA(cudaStreamBeginCaptureToGraph(s, delbody, nullptr, nullptr, 0,
                                           cudaStreamCaptureModeThreadLocal));
     launch_remove(l, c->bufs, dim);
+    const long long n_remove = dummy - n_attempt;
     CB_CUDA(cudaStreamEndCapture(s, &out));
     CB_CUDA(cudaStreamBeginCaptureToGraph(s, searchbody, nullptr, nullptr, 0,
                                           cudaStreamCaptureModeThreadLocal));
     launch_search(l, c->bufs, dim);
+    c->graph_kernels.attempt = n_attempt;
+    c->graph_kernels.remove = n_remove;
+    c->graph_kernels.search = dummy - n_attempt - n_remove;
     CB_CUDA(cudaStreamEndCapture(s, &out));
     CB_CUDA(cudaGraphInstantiate(&c->gexec, g, 0));
     // upload now, so that the first integrate's launch does not carry it
@@ -319,9 +324,9 @@ int integrate_graph(cb_context *c, int64_t n_steps) {
     CB_CUDA(cudaGraphLaunch(c->gexec, c->stream));
     rc = c->pull();
     if (rc) return rc;
-    c->launches += (h.attempts - a0) * kKernelsPerAttempt +
-                   (h.searches - s0) * kKernelsPerSearch +
-                   (h.delete_events - d0) * kKernelsPerRemove;
+    c->launches += (h.attempts - a0) * c->graph_kernels.attempt +
+                   (h.searches - s0) * c->graph_kernels.search +
+                   (h.delete_events - d0) * c->graph_kernels.remove;
     if (h.graph_mode) {  // the loop did not run to its end (a launch failure)
         h.graph_mode = 0;
         if ((rc = c->push())) return rc;

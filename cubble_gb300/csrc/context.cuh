@@ -13,10 +13,12 @@
 namespace cbg {
 int fail(int code, const std::string &msg);
 const char *status_text(int s);
-// Kernels per phase (for the launch counter of graph executions).
-constexpr int kKernelsPerAttempt = 3;
-constexpr int kKernelsPerRemove = 9;
-constexpr int kKernelsPerSearch = 16;
+// Kernels per phase of a captured graph (attempt, removal, search), counted
+// while the graph is captured; graph executions add them to the launch
+// counter per attempt, deletion and search the device reports.
+struct PhaseKernels {
+    long long attempt = 0, remove = 0, search = 0;
+};
 // Count of C-ABI calls that may touch a context, process wide: a context
 // whose host mirror was left current by a call knows, by this count, that no
 // call has run since.
@@ -57,6 +59,7 @@ struct cb_context {
     bool loaded = false;
     cudaGraphExec_t gexec = nullptr;
     int graph_key = -1;
+    cbg::PhaseKernels graph_kernels;
     long long graph_attempts0 = 0, graph_searches0 = 0, graph_deletes0 = 0;
     // g_calls when a graph cb_integrate returned with hctrl equal to the
     // device's control block and the stream idle

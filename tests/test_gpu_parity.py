@@ -303,19 +303,24 @@ def test_energy_volume(oracle_mod, dim):
     assert max_rel(g.bubble_energies(), o.bubble_energies()) <= 1e-12
 
 
-def test_graph_matches_eager(oracle_mod):
-    cfg0, st = make("3d", use_graph=0)
-    cfg1, _ = make("3d", use_graph=1)
+@pytest.mark.parametrize("case", ["2d", "3d"])
+def test_graph_matches_eager(oracle_mod, case):
+    """The same 40 steps as one graph and as eager launches: same counts and
+    states, and the graph's launch count (kernels per attempt, deletion and
+    search, counted when the graph was captured) equal to the eager one."""
+    cfg0, st = make(case, use_graph=0)
+    cfg1, _ = make(case, use_graph=1)
     a, b = cb.GpuFoam(cfg0), cb.GpuFoam(cfg1)
     for f in (a, b):
         f.load_state(st)
         workloads.prepare(f)
+    la, lb = a.launch_count(), b.launch_count()
     ra, rb = a.integrate(40), b.integrate(40)
     for k in ("steps", "attempts", "searches", "deleted", "count"):
         assert ra[k] == rb[k], k
     sa, sb = by_index(a.get_state()), by_index(b.get_state())
     assert_rows_close(sa, sb, ["x", "y", "z", "r"], 1e-10, "graph ")
-    assert b.launch_count() > 0
+    assert b.launch_count() - lb == a.launch_count() - la > 0
 
 
 @pytest.mark.parametrize("precision", [0, 2])
