@@ -676,16 +676,18 @@ CB_KERNEL_PAIR((template <int DIM>), k_pair_rows, (<DIM>), __launch_bounds__(kBl
 // cell's stencil offset times the cell edge, across a periodic face too
 // (four or more cells per axis make the offset unique): the FP32 rounding
 // is relative to a cell edge, not to the box, and the guard band where the
-// reference's FP64 test decides is ~40x narrower. The home cell's bubbles are
-// then broadcast from shared memory one at a time and every lane tests its
+// reference's FP64 test decides is ~40x narrower. A candidate out of reach
+// of the box around the home bubbles is dropped, the kept ones are packed
+// (in candidate order) into chunks of 32. The home cell's bubbles are then
+// broadcast from shared memory one at a time and every lane tests its
 // candidate against the bubble; the warp's hit mask of each (bubble, chunk)
-// goes to shared memory, and after a window of up to kTileChunks chunks each
-// lane walks the masks of its home bubble and appends the partners to the
-// bubble's row in candidate order, the order of the thread pass, so stash,
-// counts and pair list are the same. All lanes work on every test, against
-// a thread per bubble that walks its own cells with, in 3D, less than half
-// of its warp's lanes busy.
-constexpr int kTileChunks = 16;  // candidate window: 16 chunks of 32
+// goes to shared memory, and after a window of up to kTileChunks tested
+// chunks each lane walks the masks of its home bubble and appends the
+// partners to the bubble's row in candidate order, the order of the thread
+// pass, so stash, counts and pair list are the same. All lanes work on every
+// test, against a thread per bubble that walks its own cells with, in 3D,
+// less than half of its warp's lanes busy.
+constexpr int kTileChunks = 16;  // window: 16 tested chunks of 32
 
 // The tests of one chunk against home bubbles 0..nh-1 (home cell bubbles
 // among the candidates: CMP, the j > i order test): the warp's hit mask of
@@ -716,7 +718,7 @@ __device__ __forceinline__ bool tile_tests(const float4 *home, int nh, int h0, i
 // The FP64 test of the reference for the guard-band pairs of a chunk: the
 // chunk's tests are repeated and each band pair's bit set by the exact
 // decision (comparePair, src/kernels.cu:619-623). Rare: with the
-// cell-relative band about one chunk in 1500 at N = 10^6.
+// cell-relative band about 300 tests per search at N = 10^6.
 template <int DIM>
 __device__ __forceinline__ void tile_exact(const DevConst &k, const float4 *home, int nh, int h0,
                                            int j, float4 pj, float wj, float tb, unsigned *masks,
