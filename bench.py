@@ -553,7 +553,9 @@ def long_horizon_errors(args, steps, every):
         curve.append({"step": done, "energy_fp64": ea, "energy_mixed": eb,
                       "energy_rel": abs(eb / ea - 1.0),
                       "volume_drift": abs(b.total_volume() / a.total_volume() - 1.0),
-                      "per_step_max": max(v for k, v in err.items() if k != "max_error_rel")})
+                      "per_step_max": max(v for k, v in err.items()
+                                          if k not in ("max_error_rel", "max_error_vs_tol")),
+                      "error_estimate_vs_tol": err["max_error_vs_tol"]})
         if done >= steps:
             break
         a.integrate(every)
@@ -573,8 +575,9 @@ def long_horizon_errors(args, steps, every):
                         "1e-12 per step) on the same input",
            "error_definition": "per step: one attempt of each form from the FP64 run's state "
                                "every sample; max over bubbles |mixed - fp64| / max |fp64| per "
-                               "row (positions, radii: their change over the attempt); the error "
-                               "estimate relative to the tolerance (max_error_vs_tol) and to "
+                               "row (positions, radii: their change over the attempt; "
+                               "per_step_max: the largest row); the error estimate relative to "
+                               "the tolerance (max_error_vs_tol, error_estimate_vs_tol) and to "
                                "itself (max_error_rel, a difference of nearly equal FP32 rates)"}
     for f in (a, b, p64, pmx):
         f.close()

@@ -23,9 +23,12 @@
 // separation (also for nearly coincident bubbles); the minimum image on a
 // periodic axis is an integer compare against half the box
 // (wrappedDifference, src/kernels.cu:1094-1114). Only the final conversion of
-// the difference to FP32 rounds (relative 2^-24). The packed predicted state
-// is 32 bytes per bubble (q_x, q_y, q_z, r_p, 1/r_p) and the pair kernel adds
-// its results with 16-byte vector FP32 reductions.
+// the difference to FP32 rounds (relative 2^-24). The predicted radius is
+// fixed point too, so the overlap product (r_1 + r_2)^2 - d^2, a difference
+// of nearly equal squares for the shallow overlaps of a foam, is formed from
+// exact integers (overlap_product). The packed predicted state is 32 bytes
+// per bubble (q_x, q_y, q_z, q_r) and the pair kernel adds its results with
+// 16-byte vector FP32 reductions.
 #include "common.cuh"
 
 namespace cbg {
@@ -110,10 +113,11 @@ __device__ __forceinline__ void red_add4(float4 *p, float a, float b, float c, f
                  : "memory");
 }
 
-// Predicted state of one bubble in the mixed form (32 bytes).
+// Predicted state of one bubble in the mixed form (32 bytes): position and
+// radius as fixed point x 2^40.
 struct __align__(16) PredMx {
     long long q[3];
-    float r, inv;
+    long long qr;
 };
 
 // One 32-byte load per record (a 256-bit vector load; records are 32-byte
@@ -129,17 +133,18 @@ __device__ __forceinline__ PredMx ld_pred(const double *base, int i) {
     r.q[0] = a;
     r.q[1] = b;
     r.q[2] = c;
-    r.r = __int_as_float((int)(d & 0xffffffffLL));
-    r.inv = __int_as_float((int)(d >> 32));
+    r.qr = d;
     return r;
 }
 
 __device__ __forceinline__ void st_pred(double *base, int i, const PredMx &r) {
     longlong2 *p = reinterpret_cast<longlong2 *>(base) + 2 * (size_t)i;
     p[0] = make_longlong2(r.q[0], r.q[1]);
-    p[1] = make_longlong2(r.q[2], (long long)(unsigned int)__float_as_int(r.r) |
-                                      ((long long)__float_as_int(r.inv) << 32));
+    p[1] = make_longlong2(r.q[2], r.qr);
 }
+
+// The predicted radius as FP32 (one rounding of the fixed-point value).
+__device__ __forceinline__ float pred_r(const PredMx &p) { return len_from_fix(p.qr); }
 
 // The prediction the coming attempt uses: slot 0 (k_predict_mx) or one of
 // the two candidates the last correct wrote.
@@ -195,11 +200,9 @@ __device__ __forceinline__ void k_predict_mx_body(const Bufs &b, const int vb, c
             p.q[0] = fix_from_double(x[u]) + fix_from_float(h * d[0][u]);
             p.q[1] = fix_from_double(y[u]) + fix_from_float(h * d[1][u]);
             p.q[2] = DIM == 3 ? fix_from_double(z[u]) + fix_from_float(h * d[2][u]) : 0LL;
-            float rp = float_from_double(r[u]);
-            if (gas) rp = fmaf(h, d[3][u], rp);
-            p.r = rp;
-            p.inv = 1.f / rp;
+            p.qr = fix_from_double(r[u]) + (gas ? fix_from_float(h * d[3][u]) : 0LL);
             st_pred(b.pred, ii[u], p);
+            const float rp = pred_r(p);
             if (gas) {
                 const float apr = DIM == 3 ? (4.f * (float)kPi) * rp : 2.f * (float)kPi;
                 sA = fmaf(apr, rp, sA);
@@ -262,6 +265,41 @@ __device__ __forceinline__ void pair_diff(const PredMx &a, const PredMx &q, cons
     if (DIM == 3) m = fmaf(dz, dz, m);
 }
 
+// A 64-bit integer as FP32 on the integer pipe (two 32-bit conversions and
+// an FMA; the 64-bit conversion would run on the FP64 unit).
+__device__ __forceinline__ float f32_from_i64(long long v) {
+    const unsigned long long a = (unsigned long long)(v < 0 ? -v : v);
+    const float f = fmaf(__uint2float_rn((unsigned int)(a >> 32)), 4294967296.f,
+                         __uint2float_rn((unsigned int)a));
+    return v < 0 ? -f : f;
+}
+
+// (r_1 + r_2)^2 - d^2 of an overlapping pair from exact integers. For shallow
+// overlaps it is a difference of nearly equal squares, and its FP32 form
+// fmaf(R, R, -d^2) carries the roundings of d^2 and of the radii, ~10^-7 R^2,
+// into the overlap velocity f0 (R - |d|) / (|d| R) and the lens area. Here the
+// fixed-point differences e and radius sum rq (units 2^-40) are split as
+// v = h 2^20 + l (0 <= l < 2^20), so that, in units 2^-80,
+//   rq^2 - sum e^2 = (h_r^2 - sum h^2) 2^40 + 2 (h_r l_r - sum h l) 2^20 + (l_r^2 - sum l^2),
+// the first two brackets exact in 64-bit integers while the radius sum is
+// below 2^44 (16 length units; the pair overlaps, so every |e| is below it
+// too); the third, below 2^-38 absolute, is left out. One FP32 rounding of
+// the result. Larger radii take the FP32 expression.
+__device__ __forceinline__ float overlap_product(long long ex, long long ey, long long ez,
+                                                 long long rq, float radii, float m) {
+    if (rq >= (1LL << 44)) return fmaf(radii, radii, -m);
+    const int hx = (int)(ex >> 20), hy = (int)(ey >> 20), hz = (int)(ez >> 20),
+              hr = (int)(rq >> 20);
+    const int lx = (int)(ex & 0xfffff), ly = (int)(ey & 0xfffff), lz = (int)(ez & 0xfffff),
+              lr = (int)(rq & 0xfffff);
+    const long long k1 = (long long)hr * hr -
+                         ((long long)hx * hx + (long long)hy * hy + (long long)hz * hz);
+    const long long k2 = (long long)hr * lr -
+                         ((long long)hx * lx + (long long)hy * ly + (long long)hz * lz);
+    return fmaf(f32_from_i64(k2), 1.7347234759768071e-18f /* 2^-59 */,
+                f32_from_i64(k1) * kFixInv);
+}
+
 // Overlap area of an overlapping pair (src/kernels.cu:236-256): min(r1, r2)^2
 // (3D, times pi) or 2 min(r1, r2) (2D) when one centre lies inside the other
 // bubble, else from the squared half chord a^2. The reference evaluates
@@ -269,13 +307,13 @@ __device__ __forceinline__ void pair_diff(const PredMx &a, const PredMx &q, cons
 // small bubble sits on a large one (1.69 - 1.68 for radii 0.1 and 1.3); the
 // same quantity is evaluated here in the product form of the height of the
 // triangle (r1, r2, d), a^2 = ((r1 + r2)^2 - d^2) (d^2 - (r1 - r2)^2) / (4 d^2),
-// whose two factors carry the FP32 rounding of d^2 and the radii only.
+// whose two factors carry the FP32 rounding of d^2 and the radii only; p =
+// (r1 + r2)^2 - d^2 comes from overlap_product.
 template <int DIM>
 __device__ __forceinline__ float overlap_area(float r1, float r2, float r1sq, float r2sq,
-                                              float radii, float m, float rs, bool inside) {
+                                              float p, float m, float rs, bool inside) {
     if (inside) return DIM == 3 ? fminf(r1sq, r2sq) * (float)kPi : 2.f * fminf(r1, r2);
     const float rd = r1 - r2;
-    const float p = fmaf(radii, radii, -m);
     const float q = fmaf(-rd, rd, m);
     const float oa = fabsf(p * q * (0.25f * (rs * rs)));
     return DIM == 3 ? oa * (float)kPi : 2.f * sqrtf(oa);
@@ -325,14 +363,16 @@ __device__ __forceinline__ float2 recheck_containment(const int2 *RC, double *co
         long long ex, ey, ez;
         float dx, dy, dz, m;
         pair_diff<DIM>(a, q, fb, ex, ey, ez, dx, dy, dz, m);
-        const float r1 = a.r, r2 = q.r, r1sq = r1 * r1, r2sq = r2 * r2;
+        const float r1 = pred_r(a), r2 = pred_r(q), r1sq = r1 * r1, r2sq = r2 * r2;
         const bool fast = m < fmaxf(r1sq, r2sq);
         const bool exact = contained_exact(ex, ey, ez, pr.x, pr.y, ds, c);
         if (fast == exact) continue;
         const float rs = rsqrtf(m), radii = r1 + r2;
-        const float d = overlap_area<DIM>(r1, r2, r1sq, r2sq, radii, m, rs, exact) -
-                        overlap_area<DIM>(r1, r2, r1sq, r2sq, radii, m, rs, fast);
-        const float dg = d * (q.inv - a.inv);
+        const float pp = overlap_product(ex, ey, ez, a.qr + q.qr, radii, m);
+        const float d = overlap_area<DIM>(r1, r2, r1sq, r2sq, pp, m, rs, exact) -
+                        overlap_area<DIM>(r1, r2, r1sq, r2sq, pp, m, rs, fast);
+        const float inv1 = __fdividef(1.f, r1), inv2 = __fdividef(1.f, r2);
+        const float dg = d * (inv2 - inv1);
         if (DIM == 3) {
             atomicAdd(AO + pr.x, d);
             atomicAdd(AO + pr.y, d);
@@ -343,7 +383,7 @@ __device__ __forceinline__ float2 recheck_containment(const int2 *RC, double *co
             red_add4(AV + pr.y, 0.f, 0.f, d, -dg);
         }
         so += d;
-        sor = fmaf(d, a.inv + q.inv, sor);
+        sor = fmaf(d, inv1 + inv2, sor);
     }
     return make_float2(so, sor);
 }
@@ -409,6 +449,10 @@ __device__ __forceinline__ void k_pairs_mx_body(const Bufs &b, const int vb, con
         }
         int cur = -1;
         PredMx a;
+        // i's predicted radius and its reciprocal (the reciprocals of the gas
+        // flux to ~2 ulp: the flux sums carry that into the radius rates at
+        // ~10^-7 of their row maximum)
+        float r1 = 0.f, inv1 = 0.f;
         float ax = 0.f, ay = 0.f, az = 0.f, ag = 0.f, ao = 0.f;
         float fx_i = 0.f, fy_i = 0.f, fz_i = 0.f, vxi = 0.f, vyi = 0.f, vzi = 0.f;
         bool hit = false;
@@ -429,6 +473,8 @@ __device__ __forceinline__ void k_pairs_mx_body(const Bufs &b, const int vb, con
                 if (hit) flush();
                 cur = i;
                 a = ld_pred(PB, i);
+                r1 = pred_r(a);
+                if (GAS) inv1 = __fdividef(1.f, r1);
                 ax = ay = az = ag = ao = 0.f;
                 fx_i = fy_i = fz_i = 0.f;
                 hit = false;
@@ -444,12 +490,14 @@ __device__ __forceinline__ void k_pairs_mx_body(const Bufs &b, const int vb, con
             long long ex, ey, ez;
             float dx, dy, dz, m;
             pair_diff<DIM>(a, q, fb, ex, ey, ez, dx, dy, dz, m);
-            const float r1 = a.r, r2 = q.r;
+            const float r2 = pred_r(q);
             const float radii = r1 + r2;
             if (radii * radii >= m) {
-                // velocity f0 d (1/|d| - 1/(r1 + r2)), src/kernels.cu:218-233
+                // velocity f0 d (1/|d| - 1/(r1 + r2)), src/kernels.cu:218-233, as
+                // f0 d ((r1 + r2)^2 - d^2) / (|d| (r1 + r2) (r1 + r2 + |d|))
                 const float rs = rsqrtf(m);
-                const float s = f0 * (rs - __fdividef(1.f, radii));
+                const float pp = overlap_product(ex, ey, ez, a.qr + q.qr, radii, m);
+                const float s = f0 * __fdividef(pp * rs, radii * fmaf(m, rs, radii));
                 const float fx = dx * s, fy = dy * s, fz = dz * s;
                 float gf = 0.f, oa = 0.f;
                 if (GAS) {  // pairwise gas exchange, src/kernels.cu:236-280
@@ -460,10 +508,11 @@ __device__ __forceinline__ void k_pairs_mx_body(const Bufs &b, const int vb, con
                         const int e = atomicAdd(&RC[0].x, 1);
                         if (e < recheck_cap(cap)) RC[1 + e] = make_int2(i, j);
                     }
-                    oa = overlap_area<DIM>(r1, r2, r1sq, r2sq, radii, m, rs, m < rm);
-                    gf = oa * (q.inv - a.inv);
+                    oa = overlap_area<DIM>(r1, r2, r1sq, r2sq, pp, m, rs, m < rm);
+                    const float inv2 = __fdividef(1.f, r2);
+                    gf = oa * (inv2 - inv1);
                     sAo += oa;
-                    sAor = fmaf(oa, a.inv + q.inv, sAor);
+                    sAor = fmaf(oa, inv1 + inv2, sAor);
                 }
                 ax += fx;
                 ay += fy;
@@ -757,7 +806,7 @@ __device__ __forceinline__ void k_correct_mx_body(const Bufs &b, const int vb, c
             const long long q2 = DIM == 3 ? fix_from_double(cz) : 0LL;
             const float d0 = fmaf(3.f, vpx, -vx), d1 = fmaf(3.f, vpy, -vy);
             const float d2 = DIM == 3 ? fmaf(3.f, vpz, -vz) : 0.f;
-            const float rb = float_from_double(GAS ? cr_keep : r0);
+            const long long qb = fix_from_double(GAS ? cr_keep : r0);
             const float d3 = GAS ? fmaf(3.f, vpr, -vr) : 0.f;
 #pragma unroll
             for (int u = 0; u < 2; u++) {
@@ -766,10 +815,9 @@ __device__ __forceinline__ void k_correct_mx_body(const Bufs &b, const int vb, c
                 p.q[0] = q0 + fix_from_float(hh * d0);
                 p.q[1] = q1 + fix_from_float(hh * d1);
                 p.q[2] = DIM == 3 ? q2 + fix_from_float(hh * d2) : 0LL;
-                const float rp1 = GAS ? fmaf(hh, d3, rb) : rb;
-                p.r = rp1;
-                p.inv = 1.f / rp1;
+                p.qr = GAS ? qb + fix_from_float(hh * d3) : qb;
                 st_pred(b.predc + (size_t)u * 4 * cap, i, p);
+                const float rp1 = pred_r(p);
                 if (GAS) {
                     const float apr = DIM == 3 ? (4.f * (float)kPi) * rp1 : 2.f * (float)kPi;
                     if (u) {
@@ -842,8 +890,7 @@ __global__ void __launch_bounds__(kBlock) k_boot_mx(Bufs b, int phase) {
             p.q[0] = fix_from_double(X[i]);
             p.q[1] = fix_from_double(Y[i]);
             p.q[2] = DIM == 3 ? fix_from_double(Z[i]) : 0LL;
-            p.r = float_from_double(R[i]);
-            p.inv = 1.f / p.r;
+            p.qr = fix_from_double(R[i]);
             st_pred(b.pred, i, p);
             O0[i] = O1[i] = O2[i] = O3[i] = 0.f;
             PATH[i] = 0.0;

@@ -142,6 +142,42 @@ def test_c2_mixed_attempt(oracle_mod, c2):
     o.close()
 
 
+def test_c2_mixed_attempt_relaxed(c2):
+    """The mixed form's attempt late in a run, where the relaxing foam's net
+    velocities have fallen ~10x below its pair forces: the FP64 form (equal
+    to the oracle within 1e-12 per step, the tests above) runs 1500 accepted
+    steps, then one attempt of each form from that state. Every row within
+    1e-6 of its largest magnitude, as on the fresh foam; the error estimate
+    (a difference of nearly equal FP32 rates) within 1e-4 of the tolerance."""
+    cfg, st = c2
+    a = cb.GpuFoam(cfg)
+    a.load_state(st)
+    workloads.prepare(a)
+    a.integrate(1500)
+    s = a.get_state()
+    i, j = a.pairs()
+    dt = a.report()["time_step"]
+    ref = cb.GpuFoam(cfg)
+    g = cb.GpuFoam(workloads.sweep_config_as(cfg, precision=1))
+    for f in (ref, g):
+        f.load_state(s)
+        f.set_pairs(i, j)
+        f.set_time(dt)
+    ag, ar = g.attempt(), ref.attempt()
+    lim = 1e-6
+    for k, base in (("xp", "x"), ("yp", "y"), ("zp", "z"), ("rp", "r")):
+        assert max_rel(ag[k] - s[base], ar[k] - s[base]) <= lim, k
+    for k in ("dxdtp", "dydtp", "dzdtp", "drdtp", "overlap", "path_new"):
+        assert max_rel(ag[k], ar[k]) <= lim, k
+    for k in ("total_area", "total_area_per_radius", "total_overlap_area",
+              "total_overlap_area_per_radius", "total_volume_new"):
+        assert ag[k] == pytest.approx(ar[k], rel=lim), k
+    assert abs(ag["max_error"] - ar["max_error"]) <= 1e-4 * cfg.error_tolerance
+    assert np.array_equal(ag["delete_flags"], ar["delete_flags"])
+    for f in (a, ref, g):
+        f.close()
+
+
 def test_c2_every_step(oracle_mod, c2):
     """60 accepted steps of the 3D N = 10^6 foam with the CUDA path and the
     oracle in lockstep, compared after every step: the same attempt, search
