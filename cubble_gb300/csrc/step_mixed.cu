@@ -143,8 +143,14 @@ __device__ __forceinline__ void st_pred(double *base, int i, const PredMx &r) {
     p[1] = make_longlong2(r.q[2], r.qr);
 }
 
-// The predicted radius as FP32 (one rounding of the fixed-point value).
-__device__ __forceinline__ float pred_r(const PredMx &p) { return len_from_fix(p.qr); }
+// The predicted radius as FP32 (one rounding of the fixed-point value, which
+// is >= 0).
+__device__ __forceinline__ float pred_r(const PredMx &p) {
+    const unsigned long long a = (unsigned long long)p.qr;
+    return fmaf(__uint2float_rn((unsigned int)(a >> 32)), 4294967296.f,
+                __uint2float_rn((unsigned int)a)) *
+           kFixInv;
+}
 
 // The prediction the coming attempt uses: slot 0 (k_predict_mx) or one of
 // the two candidates the last correct wrote.
@@ -283,8 +289,9 @@ __device__ __forceinline__ float f32_from_i64(long long v) {
 //   rq^2 - sum e^2 = (h_r^2 - sum h^2) 2^40 + 2 (h_r l_r - sum h l) 2^20 + (l_r^2 - sum l^2),
 // the first two brackets exact in 64-bit integers while the radius sum is
 // below 2^44 (16 length units; the pair overlaps, so every |e| is below it
-// too); the third, below 2^-38 absolute, is left out. One FP32 rounding of
-// the result. Larger radii take the FP32 expression.
+// too); the third, below 2^-38 absolute, is left out, and the second enters
+// to 2^19 of its units (2^-40 absolute). One FP32 rounding of the result.
+// Larger radii take the FP32 expression.
 __device__ __forceinline__ float overlap_product(long long ex, long long ey, long long ez,
                                                  long long rq, float radii, float m) {
     if (rq >= (1LL << 44)) return fmaf(radii, radii, -m);
@@ -296,8 +303,7 @@ __device__ __forceinline__ float overlap_product(long long ex, long long ey, lon
                          ((long long)hx * hx + (long long)hy * hy + (long long)hz * hz);
     const long long k2 = (long long)hr * lr -
                          ((long long)hx * lx + (long long)hy * ly + (long long)hz * lz);
-    return fmaf(f32_from_i64(k2), 1.7347234759768071e-18f /* 2^-59 */,
-                f32_from_i64(k1) * kFixInv);
+    return f32_from_i64(k1 + (k2 >> 19)) * kFixInv;
 }
 
 // Overlap area of an overlapping pair (src/kernels.cu:236-256): min(r1, r2)^2
