@@ -14,7 +14,9 @@
 // float <-> double, int64 -> float) on one unit at 1/64 of the FP32 rate.
 // The mixed kernels therefore convert on the integer pipe, from the IEEE-754
 // bit patterns (fix_from_double, fix_from_float, double_from_float,
-// float_from_double below), and use FP64 arithmetic only for the position,
+// float_from_double below; float_rn_from_double, rounded to nearest, where a
+// conversion toward zero would bias every bubble alike), and use FP64
+// arithmetic only for the position,
 // radius and path updates, the differences to the saved position and the
 // volume sum (12 FP64 instructions per bubble in 3D).
 //
