@@ -872,15 +872,17 @@ __device__ __forceinline__ void k_pair_tiles_body(const Bufs &b, const int vb, c
                 ph = pos[h0 + lane];
                 home[w][lane] = ph;
             }
-            // the box around the home bubbles and their largest radius: a
-            // candidate farther from the box than that radius + its own +
-            // skin + pad pairs with none of them, and is dropped before the
-            // tests (pad = 4 band covers the FP32 error of the tests, so the
-            // exact test would refuse every dropped pair)
+            // the box around the home bubbles (each centre +- its radius): a
+            // candidate farther from the box than its own radius + skin + pad
+            // is farther than r_i + r_j + skin + pad from every home centre,
+            // pairs with none of them, and is dropped before the tests (pad
+            // = 4 band covers the FP32 error of the tests, so the exact test
+            // would refuse every dropped pair)
             const bool hv = lane < nh;
-            float blo[3] = {hv ? ph.x : 3.4e38f, hv ? ph.y : 3.4e38f, hv ? ph.z : 3.4e38f};
-            float bhi[3] = {hv ? ph.x : -3.4e38f, hv ? ph.y : -3.4e38f, hv ? ph.z : -3.4e38f};
-            float rh = hv ? ph.w : 0.f;
+            float blo[3] = {hv ? ph.x - ph.w : 3.4e38f, hv ? ph.y - ph.w : 3.4e38f,
+                            hv ? ph.z - ph.w : 3.4e38f};
+            float bhi[3] = {hv ? ph.x + ph.w : -3.4e38f, hv ? ph.y + ph.w : -3.4e38f,
+                            hv ? ph.z + ph.w : -3.4e38f};
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
 #pragma unroll
@@ -888,9 +890,8 @@ __device__ __forceinline__ void k_pair_tiles_body(const Bufs &b, const int vb, c
                     blo[a] = fminf(blo[a], __shfl_xor_sync(kAll, blo[a], o));
                     bhi[a] = fmaxf(bhi[a], __shfl_xor_sync(kAll, bhi[a], o));
                 }
-                rh = fmaxf(rh, __shfl_xor_sync(kAll, rh, o));
             }
-            const float reach0 = rh + skin + 4.f * band;
+            const float reach0 = skin + 4.f * band;
             __syncwarp();
             int mycnt = 0;  // partners of home bubble h0 + lane so far
             int *row = stash + (size_t)(h0 + min(lane, nh - 1)) * M;
