@@ -45,6 +45,37 @@ def mixed_from(o, dim, n, **kw):
     return g
 
 
+def test_mixed_large_radii(oracle_mod):
+    """Radii of 6-12 length units: most overlapping pairs have r1 + r2 above
+    16, where the overlap product (r1 + r2)^2 - d^2 is no longer formed from
+    exact integers and the FP32 expression is used; one attempt against the
+    oracle at the same bars as the unit-radius foams."""
+    cfg, st = workloads.foam(3000, 3, 0.8, rmean=9.0, rstd=1.0, rclip=(6.0, 12.0), seed=43)
+    o = oracle_mod.OracleFoam(cfg)
+    o.load_state(st)
+    workloads.prepare(o)
+    o.integrate(5)
+    s = o.get_state()
+    cfg_m, _ = workloads.foam(3000, 3, 0.8, rmean=9.0, rstd=1.0, rclip=(6.0, 12.0), seed=43,
+                              precision=1)
+    g = cb.GpuFoam(cfg_m)
+    g.load_state(s)
+    i, j = o.pairs()
+    g.set_pairs(i, j)
+    g.set_time(o.report()["time_step"])
+    ag, ao = g.attempt(), o.attempt()
+    lim = 1e-6
+    for k, base in (("xp", "x"), ("yp", "y"), ("zp", "z"), ("rp", "r")):
+        assert max_rel(ag[k] - s[base], ao[k] - s[base]) <= lim, k
+    for k in ("dxdtp", "dydtp", "dzdtp", "drdtp", "overlap", "path_new"):
+        assert max_rel(ag[k], ao[k]) <= lim, k
+    for k in ("total_area", "total_area_per_radius", "total_overlap_area",
+              "total_overlap_area_per_radius"):
+        assert ag[k] == pytest.approx(ao[k], rel=lim), k
+    g.close()
+    o.close()
+
+
 @pytest.mark.parametrize("dim", [3, 2])
 def test_mixed_single_attempt(oracle_mod, dim):
     cfg, o = prepared(oracle_mod, dim, 8000)
