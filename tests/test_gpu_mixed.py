@@ -45,6 +45,35 @@ def mixed_from(o, dim, n, **kw):
     return g
 
 
+def test_mixed_volume_over_200_steps():
+    """The benchmark's foam at N = 10^5: the mixed and the FP64 forms run 200
+    accepted steps from the same prepared state, with no deletion in between
+    to reset the volumes. Each form's total gas volume moves (the AM2 radius
+    update conserves it to first order); the mixed form must follow the FP64
+    one to 3e-11 — values that enter every bubble's update alike (half step,
+    mean-field factor, the radius of the gas-exchange term) rounded toward
+    zero instead of to nearest made it ~1e-10 by this step at N = 10^6."""
+    cfg, st = workloads.config_c2(n=100_000, use_graph=1)
+    a = cb.GpuFoam(cfg)
+    a.load_state(st)
+    workloads.prepare(a)
+    a.integrate(3)
+    s0 = a.get_state()
+    i, j = a.pairs()
+    dt = a.report()["time_step"]
+    b = cb.GpuFoam(workloads.sweep_config_as(cfg, precision=1))
+    b.load_state(s0)
+    b.set_pairs(i, j)
+    b.set_time(dt)
+    a.set_time(dt)
+    ra0, rb0 = a.report(), b.report()
+    ra, rb = a.integrate(200), b.integrate(200)
+    assert ra["deleted"] == ra0["deleted"] and rb["deleted"] == rb0["deleted"]
+    assert b.total_volume() == pytest.approx(a.total_volume(), rel=3e-11)
+    a.close()
+    b.close()
+
+
 def test_mixed_large_radii(oracle_mod):
     """Radii of 6-12 length units: most overlapping pairs have r1 + r2 above
     16, where the overlap product (r1 + r2)^2 - d^2 is no longer formed from
